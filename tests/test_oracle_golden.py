@@ -1,0 +1,66 @@
+"""The FP64 oracle against golden vectors produced by the reference itself
+(tests/golden/make_golden.py: the reference's own routines, strict FP64 build).
+
+Every comparison is exact: the oracle follows the reference's operation order.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import GOLDEN_GRAPHS, load_golden
+
+
+@pytest.fixture(scope="module", params=GOLDEN_GRAPHS)
+def gold(request):
+    return request.param, load_golden(request.param)
+
+
+@pytest.mark.parametrize("algo", [2, 3, 4, 6, 8])
+@pytest.mark.parametrize("iters", [1, 4])
+def test_layout_bit_exact(gold, algo, iters):
+    _, z = gold
+    out, e, loops, f = oracle.layout(algo, z["csr_rowptr"], z["csr_colids"], z["init_xy"], iters, 32,
+                                     want_forces=True, nthreads=1)
+    assert np.array_equal(out, z[f"L{algo}_i{iters}_xy"])
+    assert np.array_equal(f, z[f"L{algo}_i{iters}_f"])
+    assert e == float(z[f"L{algo}_i{iters}_e"])
+
+
+def test_layout_threads_do_not_change_result(gold):
+    _, z = gold
+    a = oracle.layout(2, z["csr_rowptr"], z["csr_colids"], z["init_xy"], 4, 32, nthreads=1)
+    b = oracle.layout(2, z["csr_rowptr"], z["csr_colids"], z["init_xy"], 4, 32, nthreads=4)
+    assert np.array_equal(a[0], b[0]) and a[1] == b[1]
+
+
+def test_converged_bit_exact(gold):
+    _, z = gold
+    out, e, loops = oracle.layout(2, z["csr_rowptr"], z["csr_colids"], z["init_xy"], 600, 32, engt=0.05,
+                                  nthreads=1)
+    assert loops == int(z["conv_loops"])
+    assert e == float(z["conv_e"])
+    assert np.array_equal(out, z["conv_xy"])
+
+
+def test_morton_sort_matches_reference(gold):
+    _, z = gold
+    xy = z["init_xy"]
+    _, keys, perm = oracle.morton_sort(xy)
+    assert np.array_equal(xy[perm], z["bh_sorted"])
+    assert np.all(np.diff(keys.astype(np.float64)) >= 0)
+
+
+def test_tree_matches_reference(gold):
+    _, z = gold
+    t = oracle.bh_tree(z["init_xy"])
+    for k in ("lo", "hi", "depth", "nchild"):
+        assert np.array_equal(t[k], z["tree_" + k]), k
+    assert np.array_equal(t["centroid"], z["tree_centroid"])
+
+
+@pytest.mark.parametrize("theta", [1.2, 0.5])
+def test_bh_repulsion_matches_reference(gold, theta):
+    _, z = gold
+    xy = z["init_xy"]
+    r = oracle.bh_repulsion(xy, xy, theta, nthreads=2)
+    assert np.array_equal(r, z[f"bh_rep_t{theta}"])
