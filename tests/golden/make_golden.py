@@ -40,8 +40,8 @@ ALGOS = (2, 3, 4, 6, 8)
 ITERS = (1, 4)
 
 
-def run(args):
-    r = subprocess.run(args, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, check=True)
+def run(args, cwd=None):
+    r = subprocess.run(args, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, check=True, cwd=cwd)
     if os.path.basename(args[0]) != "ref_driver":
         return r.stdout
     # the reference reader prints its progress with printf (IO.h:147-148)
@@ -176,7 +176,7 @@ def main():
     with tempfile.TemporaryDirectory() as td:
         mtx = os.path.join(HERE, "grid12.mtx")
         out = run([stock, "-input", mtx, "-output", td + "/", "-iter", "3", "-algo", "2", "-threads", "1",
-                   "-initf", os.path.join(HERE, "grid12.initf"), "-batch", str(BATCH)])
+                   "-initf", os.path.join(HERE, "grid12.initf"), "-batch", str(BATCH)], cwd=td)
         with open(os.path.join(HERE, "ref_stdout_grid12.txt"), "w") as f:
             f.write(out.replace(td + "/", "<OUTDIR>/").replace(HERE + "/", "<GOLDEN>/"))
         with open(os.path.join(td, "grid12.mtxCACHEMINB32PARAOUT3.txt")) as fin, \
