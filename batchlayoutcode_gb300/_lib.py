@@ -1,0 +1,319 @@
+"""ctypes binding of libbatchlayout_gb300.so (include/batchlayout_gb300.h).
+
+There is no CPU fallback: if the library is missing or the device call fails,
+the error is raised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libbatchlayout_gb300.so")
+
+# every symbol declared in include/batchlayout_gb300.h
+EXPORTS = (
+    "bl_algorithms_create", "bl_create_error", "bl_destroy", "bl_last_error", "bl_num_vertices",
+    "bl_read_matrix_market", "bl_free", "bl_set_coordinates", "bl_get_coordinates", "bl_get_forces",
+    "bl_rand_init", "bl_init_dfs", "bl_file_initialization", "bl_cache_blocking_minibatch",
+    "bl_cache_blocking_minibatch_converged", "bl_linlog_cache_blocking_minibatch",
+    "bl_fa_cache_blocking_minibatch", "bl_barnes_hut_approximation", "bl_approx_cache_block_bh",
+    "bl_write_to_file", "bl_minibatch_iteration", "bl_barnes_hut_iteration", "bl_morton_order",
+    "bl_quadtree", "bl_bh_repulsion", "bl_run_resident", "bl_set_graph_mode", "bl_last_kernel_time",
+    "bl_kernel_launches", "bl_last_run_ms", "bl_random_coordinates", "bl_greedy_coordinates", "bl_write_coordinates",
+)
+
+_lib = None
+
+
+class BatchLayoutError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"batchlayout error {code}: {msg}")
+        self.code = code
+
+
+def load() -> C.CDLL:
+    """Load the library (build it first with batchlayoutcode_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: run `python -m batchlayoutcode_gb300.build`")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64, f64, cp = C.c_void_p, C.c_int, C.c_longlong, C.c_double, C.c_char_p
+    dp = C.POINTER(C.c_double)
+    ip = C.POINTER(C.c_int)
+    sig = {
+        "bl_algorithms_create": (vp, [i32, i32, i64, ip, ip, cp, cp, i32, f64, f64, cp]),
+        "bl_create_error": (cp, []),
+        "bl_destroy": (None, [vp]),
+        "bl_last_error": (cp, [vp]),
+        "bl_num_vertices": (i32, [vp]),
+        "bl_read_matrix_market": (i32, [cp, C.POINTER(C.c_longlong), dp, C.POINTER(ip), C.POINTER(ip), cp, i32]),
+        "bl_free": (None, [vp]),
+        "bl_set_coordinates": (i32, [vp, dp, i32]),
+        "bl_get_coordinates": (i32, [vp, dp, i32]),
+        "bl_get_forces": (i32, [vp, dp, i32]),
+        "bl_rand_init": (i32, [vp]),
+        "bl_init_dfs": (i32, [vp]),
+        "bl_file_initialization": (i32, [vp]),
+        "bl_cache_blocking_minibatch": (i32, [vp, i32, i32, i32, i32, dp]),
+        "bl_cache_blocking_minibatch_converged": (i32, [vp, i32, i32, i32, i32, dp]),
+        "bl_linlog_cache_blocking_minibatch": (i32, [vp, i32, i32, i32, dp]),
+        "bl_fa_cache_blocking_minibatch": (i32, [vp, i32, i32, i32, dp]),
+        "bl_barnes_hut_approximation": (i32, [vp, i32, i32, i32, f64, i32, dp]),
+        "bl_approx_cache_block_bh": (i32, [vp, i32, i32, i32, dp]),
+        "bl_write_to_file": (i32, [vp, cp, cp, i32]),
+        "bl_minibatch_iteration": (i32, [vp, i32, i32, f64, dp]),
+        "bl_barnes_hut_iteration": (i32, [vp, i32, f64, f64, dp]),
+        "bl_morton_order": (i32, [vp, dp, C.POINTER(C.c_ulonglong), ip]),
+        "bl_quadtree": (i32, [vp, i32, ip, ip, ip, ip, dp]),
+        "bl_bh_repulsion": (i32, [vp, f64, dp, C.POINTER(C.c_longlong)]),
+        "bl_run_resident": (i32, [vp, i32, i32, i32, f64, f64, dp]),
+        "bl_set_graph_mode": (i32, [vp, i32]),
+        "bl_last_kernel_time": (i32, [vp, cp, dp]),
+        "bl_kernel_launches": (i64, [vp]),
+        "bl_last_run_ms": (i32, [vp, dp]),
+        "bl_random_coordinates": (i32, [i32, dp]),
+        "bl_greedy_coordinates": (i32, [i32, ip, ip, dp]),
+        "bl_write_coordinates": (i32, [cp, cp, cp, dp, i32, cp, i32]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def read_matrix_market(path: str):
+    """SetInputMatricesAsCSR: -> (rowptr, colids, info dict)."""
+    L = load()
+    info = (C.c_longlong * 4)()
+    secs = C.c_double()
+    rp = C.POINTER(C.c_int)()
+    ci = C.POINTER(C.c_int)()
+    err = C.create_string_buffer(512)
+    rc = L.bl_read_matrix_market(path.encode(), info, C.byref(secs), C.byref(rp), C.byref(ci), err, 512)
+    if rc != 0:
+        raise BatchLayoutError(rc, err.value.decode())
+    rows, cols, nnz, sym = (int(v) for v in info)
+    rowptr = np.ctypeslib.as_array(rp, shape=(rows + 1,)).copy()
+    colids = np.ctypeslib.as_array(ci, shape=(max(nnz, 1),))[:nnz].copy()
+    L.bl_free(C.cast(rp, C.c_void_p))
+    L.bl_free(C.cast(ci, C.c_void_p))
+    return rowptr, colids, dict(rows=rows, cols=cols, nnz=nnz, symmetric=bool(sym), seconds=secs.value)
+
+
+def random_coordinates(n: int) -> np.ndarray:
+    """randInit's sequence (one thread), host only."""
+    out = np.zeros((n, 2))
+    rc = load().bl_random_coordinates(n, _dp(out))
+    if rc != 0:
+        raise BatchLayoutError(rc, "bl_random_coordinates")
+    return out
+
+
+def greedy_coordinates(rowptr, colids) -> np.ndarray:
+    """initDFS's placement, host only."""
+    rp = np.ascontiguousarray(rowptr, dtype=np.int32)
+    ci = np.ascontiguousarray(colids, dtype=np.int32)
+    n = rp.shape[0] - 1
+    out = np.zeros((n, 2))
+    rc = load().bl_greedy_coordinates(n, _ip(rp), _ip(ci), _dp(out))
+    if rc != 0:
+        raise BatchLayoutError(rc, "bl_greedy_coordinates")
+    return out
+
+
+def write_coordinates(input: str, outputdir: str, tag: str, xy) -> str:
+    """writeToFile's naming and format, host only; returns the path written."""
+    a = np.ascontiguousarray(xy, dtype=np.float64)
+    buf = C.create_string_buffer(4096)
+    rc = load().bl_write_coordinates(input.encode(), outputdir.encode(), tag.encode(), _dp(a), a.shape[0], buf, 4096)
+    if rc != 0:
+        raise BatchLayoutError(rc, "cannot write " + buf.value.decode())
+    return buf.value.decode()
+
+
+class Algorithms:
+    """Python mirror of the reference's `class algorithms` (sample/algorithms.h:50-85)
+    over the C ABI.  Method names and arguments follow the reference."""
+
+    def __init__(self, rowptr, colids, input: str = "graph.mtx", outputd: str = "", init: int = 2,
+                 weight: float = 1.0, th: float = 0.01, ifile: str = "", device: int = 0):
+        L = load()
+        self._L = L
+        self.rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
+        self.colids = np.ascontiguousarray(colids, dtype=np.int32)
+        self.n = int(self.rowptr.shape[0] - 1)
+        ctx = L.bl_algorithms_create(device, self.n, int(self.rowptr[-1]), _ip(self.rowptr), _ip(self.colids),
+                                     input.encode(), outputd.encode(), init, weight, th, ifile.encode())
+        if not ctx:
+            raise BatchLayoutError(-1, L.bl_create_error().decode())
+        self._ctx = ctx
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._L.bl_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise BatchLayoutError(rc, self._L.bl_last_error(self._ctx).decode())
+
+    # ---- coordinates ----
+    @property
+    def nCoordinates(self) -> np.ndarray:
+        out = np.zeros((self.n, 2))
+        self._check(self._L.bl_get_coordinates(self._ctx, _dp(out), self.n))
+        return out
+
+    @nCoordinates.setter
+    def nCoordinates(self, xy):
+        a = np.ascontiguousarray(xy, dtype=np.float64).reshape(self.n, 2)
+        self._check(self._L.bl_set_coordinates(self._ctx, _dp(a), self.n))
+
+    @property
+    def prevCoordinates(self) -> np.ndarray:
+        out = np.zeros((self.n, 2))
+        self._check(self._L.bl_get_forces(self._ctx, _dp(out), self.n))
+        return out
+
+    # ---- initialisers ----
+    def randInit(self):
+        self._check(self._L.bl_rand_init(self._ctx))
+
+    def initDFS(self):
+        self._check(self._L.bl_init_dfs(self._ctx))
+
+    def fileInitialization(self):
+        self._check(self._L.bl_file_initialization(self._ctx))
+
+    # ---- layout methods (return [ENERGY, seconds]) ----
+    def _out(self, k=2):
+        return (C.c_double * k)()
+
+    def cacheBlockingminiBatchForceDirectedAlgorithm(self, ITERATIONS, NUMOFTHREADS=0, BATCHSIZE=256, flag=0):
+        o = self._out()
+        self._check(self._L.bl_cache_blocking_minibatch(self._ctx, ITERATIONS, NUMOFTHREADS, BATCHSIZE, flag, o))
+        return [o[0], o[1]]
+
+    def cacheBlockingminiBatchForceDirectedAlgorithmConverged(self, ITERATIONS, NUMOFTHREADS=0, BATCHSIZE=256,
+                                                             flag=0):
+        o = self._out(3)
+        self._check(self._L.bl_cache_blocking_minibatch_converged(self._ctx, ITERATIONS, NUMOFTHREADS, BATCHSIZE,
+                                                                  flag, o))
+        self.loops = int(o[2])
+        return [o[0], o[1]]
+
+    def LinLogcacheBlockingminiBatchForceDirectedAlgorithm(self, ITERATIONS, NUMOFTHREADS=0, BATCHSIZE=256):
+        o = self._out()
+        self._check(self._L.bl_linlog_cache_blocking_minibatch(self._ctx, ITERATIONS, NUMOFTHREADS, BATCHSIZE, o))
+        return [o[0], o[1]]
+
+    def FAcacheBlockingminiBatchForceDirectedAlgorithm(self, ITERATIONS, NUMOFTHREADS=0, BATCHSIZE=256):
+        o = self._out()
+        self._check(self._L.bl_fa_cache_blocking_minibatch(self._ctx, ITERATIONS, NUMOFTHREADS, BATCHSIZE, o))
+        return [o[0], o[1]]
+
+    def BarnesHutApproximation(self, ITERATIONS, NUMOFTHREADS=0, BATCHSIZE=256, TH=1.2, flag=0):
+        o = self._out()
+        self._check(self._L.bl_barnes_hut_approximation(self._ctx, ITERATIONS, NUMOFTHREADS, BATCHSIZE, TH, flag, o))
+        return [o[0], o[1]]
+
+    def approxCacheBlockBH(self, ITERATIONS, NUMOFTHREADS=0, BATCHSIZE=256):
+        o = self._out()
+        self._check(self._L.bl_approx_cache_block_bh(self._ctx, ITERATIONS, NUMOFTHREADS, BATCHSIZE, o))
+        return [o[0], o[1]]
+
+    def writeToFile(self, f: str) -> str:
+        buf = C.create_string_buffer(4096)
+        self._check(self._L.bl_write_to_file(self._ctx, f.encode(), buf, 4096))
+        return buf.value.decode()
+
+    # ---- building blocks ----
+    def minibatch_iteration(self, model: int, batch: int, step: float) -> float:
+        e = C.c_double()
+        self._check(self._L.bl_minibatch_iteration(self._ctx, model, batch, step, C.byref(e)))
+        return e.value
+
+    def barnes_hut_iteration(self, batch: int, theta: float, step: float) -> float:
+        e = C.c_double()
+        self._check(self._L.bl_barnes_hut_iteration(self._ctx, batch, theta, step, C.byref(e)))
+        return e.value
+
+    def morton_order(self):
+        frame = np.zeros(3)
+        keys = np.zeros(self.n, np.uint64)
+        perm = np.zeros(self.n, np.int32)
+        self._check(self._L.bl_morton_order(self._ctx, _dp(frame), keys.ctypes.data_as(C.POINTER(C.c_ulonglong)),
+                                            _ip(perm)))
+        return frame, keys, perm
+
+    def quadtree(self) -> dict:
+        cap = 2 * self.n + 8
+        lo, hi, dep, nc = (np.zeros(cap, np.int32) for _ in range(4))
+        cen = np.zeros(2 * cap)
+        m = self._L.bl_quadtree(self._ctx, cap, _ip(lo), _ip(hi), _ip(dep), _ip(nc), _dp(cen))
+        if m < 0:
+            self._check(m)
+        return dict(lo=lo[:m], hi=hi[:m], depth=dep[:m], nchild=nc[:m], centroid=cen[: 2 * m].reshape(m, 2))
+
+    def bh_repulsion(self, theta: float):
+        out = np.zeros((self.n, 2))
+        st = (C.c_longlong * 2)()
+        self._check(self._L.bl_bh_repulsion(self._ctx, theta, _dp(out), st))
+        return out, (int(st[0]), int(st[1]))
+
+    def run_resident(self, algo: int, iterations: int, batch: int = 256, theta: float = 1.2,
+                     step: float = 1.0) -> float:
+        e = C.c_double()
+        self._check(self._L.bl_run_resident(self._ctx, algo, iterations, batch, theta, step, C.byref(e)))
+        return e.value
+
+    def last_run_ms(self) -> float:
+        """CUDA-event device time of the last run_resident call."""
+        ms = C.c_double()
+        self._check(self._L.bl_last_run_ms(self._ctx, C.byref(ms)))
+        return ms.value
+
+    def set_coordinates_ptr(self, ptr: int):
+        """bl_set_coordinates from a raw host pointer (e.g. pinned memory)."""
+        self._check(self._L.bl_set_coordinates(self._ctx, C.cast(ptr, C.POINTER(C.c_double)), self.n))
+
+    def get_coordinates_ptr(self, ptr: int):
+        self._check(self._L.bl_get_coordinates(self._ctx, C.cast(ptr, C.POINTER(C.c_double)), self.n))
+
+    def set_graph_mode(self, enabled: bool):
+        self._check(self._L.bl_set_graph_mode(self._ctx, 1 if enabled else 0))
+
+    def kernel_time(self, kernel: str | None = None):
+        ms = (C.c_double * 2)()
+        self._check(self._L.bl_last_kernel_time(self._ctx, kernel.encode() if kernel else None, ms))
+        return ms[0], int(ms[1])
+
+    def kernel_launches(self) -> int:
+        return int(self._L.bl_kernel_launches(self._ctx))

@@ -1,0 +1,821 @@
+// barnes_hut.cu -- Barnes-Hut minibatch layout (algo 4) on the device.
+//
+// Reference: sample/algorithms.cpp:1038-1072 (iteration), sample/MortonCode.h
+// (frame, quantisation, order), sample/BarnesHut.h:114-225 (sort, quadtree
+// build, opening test, unit-vector repulsion).
+//
+// Per iteration:
+//   1. bbox of the positions; Morton frame {minX, minY, MAXMIN} and 64-bit keys
+//      (y-major interleave of the two 32-bit quantised coordinates, quantised
+//      in FP64 exactly as the reference: (uint32)(4294967295.0*(x-minX)/MAXMIN)).
+//   2. stable LSD radix sort of (key, vertex) pairs, 8 passes of 8 bits.
+//   3. binary radix tree over the sorted keys (Karras 2012), then a bottom-up
+//      pass that merges the x-bit level into the y-bit level of the same
+//      digit, giving exactly the reference quadtree without its single-child
+//      chain nodes; centroids are the unweighted means of the children summed
+//      in quadrant order, in FP64, bit-identical to the reference.
+//   4. pre-order layout with skip links: 16-byte records {x, y, D^2, skip}
+//      walked without a stack.
+//   5. repulsion of every vertex in Morton order (coherent warps).  A vertex
+//      is only moved by its own batch, so its query position and the tree
+//      snapshot are both the iteration-start positions: all n traversals are
+//      independent.  The opening test D/dist < theta is evaluated in FP32 and
+//      re-evaluated in FP64 when the FP32 margin is within its error bound,
+//      so every decision equals the reference's FP64 decision.
+//   6. attraction + update.  Vertex i reads the new position of a neighbour j
+//      from an earlier batch and the iteration-start position otherwise, so
+//      the batch order only constrains i after its earlier-batch neighbours:
+//      vertices are grouped into dependency levels (computed once per graph
+//      and batch size) and each level is one parallel launch.  This produces
+//      the same values as the reference's sequential batch loop.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "bl_internal.cuh"
+
+namespace bl {
+namespace {
+
+typedef unsigned long long u64;
+
+__device__ __forceinline__ unsigned int f2ord(float f) {
+  const unsigned int u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned int u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__global__ void bbox_init_kernel(unsigned int *bbox) {
+  if (threadIdx.x == 0) {
+    bbox[0] = 0xffffffffu;  // min x
+    bbox[1] = 0u;           // max x
+    bbox[2] = 0xffffffffu;  // min y
+    bbox[3] = 0u;           // max y
+  }
+}
+
+__global__ void bbox_kernel(const float2 *__restrict__ pos, int n, unsigned int *bbox) {
+  unsigned int mnx = 0xffffffffu, mxx = 0u, mny = 0xffffffffu, mxy = 0u;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float2 p = pos[i];
+    const unsigned int ux = f2ord(p.x), uy = f2ord(p.y);
+    mnx = min(mnx, ux); mxx = max(mxx, ux);
+    mny = min(mny, uy); mxy = max(mxy, uy);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mnx = min(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+    mxx = max(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+    mny = min(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+    mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&bbox[0], mnx);
+    atomicMax(&bbox[1], mxx);
+    atomicMin(&bbox[2], mny);
+    atomicMax(&bbox[3], mxy);
+  }
+}
+
+__device__ __forceinline__ u64 spread32(unsigned int v) {
+  u64 x = v;
+  x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
+  x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
+  x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
+  x = (x | (x << 2)) & 0x3333333333333333ull;
+  x = (x | (x << 1)) & 0x5555555555555555ull;
+  return x;
+}
+
+// Frame (MortonCode.h:42-52) from the bbox; FP64 like the reference.
+__device__ __forceinline__ void frame_from_bbox(const unsigned int *bbox, double &minX,
+                                                double &minY, double &maxmin) {
+  minX = (double)ord2f(bbox[0]);
+  const double maxX = (double)ord2f(bbox[1]);
+  minY = (double)ord2f(bbox[2]);
+  const double maxY = (double)ord2f(bbox[3]);
+  const double ry = __dsub_rn(maxY, minY), rx = __dsub_rn(maxX, minX);
+  maxmin = (ry < rx) ? rx : ry;  // std::max(y-range, x-range)
+}
+
+// (uint32)(4294967295.0 * (v - mn) / maxmin), MortonCode.h:62-67, no contraction
+__device__ __forceinline__ unsigned int quantise(float v, double mn, double maxmin) {
+  if (!(maxmin > 0.0)) return 0u;
+  const double q = __ddiv_rn(__dmul_rn(4294967295.0, __dsub_rn((double)v, mn)), maxmin);
+  return __double2uint_rz(q);
+}
+
+__global__ void morton_kernel(const float2 *__restrict__ pos, int n, const unsigned int *bbox,
+                              u64 *keys, int *vals, double *frame) {
+  double minX, minY, maxmin;
+  frame_from_bbox(bbox, minX, minY, maxmin);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    frame[0] = minX;
+    frame[1] = minY;
+    frame[2] = maxmin;
+  }
+  if (i >= n) return;
+  const float2 p = pos[i];
+  keys[i] = (spread32(quantise(p.y, minY, maxmin)) << 1) | spread32(quantise(p.x, minX, maxmin));
+  vals[i] = i;
+}
+
+// ---- stable LSD radix sort, 8-bit digits ------------------------------------
+constexpr int kRsThreads = 256;
+constexpr int kRsItems = 16;
+constexpr int kRsTile = kRsThreads * kRsItems;
+
+__global__ void __launch_bounds__(kRsThreads) rs_hist_kernel(const u64 *__restrict__ keys, int n,
+                                                             int shift, unsigned int *hist,
+                                                             int nblocks) {
+  __shared__ unsigned int cnt[256];
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int base = blockIdx.x * kRsTile;
+#pragma unroll 4
+  for (int r = 0; r < kRsItems; r++) {
+    const int idx = base + r * kRsThreads + threadIdx.x;
+    if (idx < n) atomicAdd(&cnt[(unsigned int)(keys[idx] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// One block of 256 threads: thread d turns row d of hist into exclusive offsets
+// across blocks, then the digit totals are scanned and added.
+__global__ void __launch_bounds__(256) rs_scan_kernel(unsigned int *hist, int nblocks) {
+  __shared__ unsigned int tot[256];
+  const int d = threadIdx.x;
+  unsigned int run = 0;
+  unsigned int *row = hist + (size_t)d * nblocks;
+  int b = 0;
+  for (; b + 8 <= nblocks; b += 8) {
+    unsigned int v[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = row[b + k];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      row[b + k] = run;
+      run += v[k];
+    }
+  }
+  for (; b < nblocks; b++) {
+    const unsigned int v = row[b];
+    row[b] = run;
+    run += v;
+  }
+  tot[d] = run;
+  __syncthreads();
+  // exclusive scan of the 256 totals (Hillis-Steele on a copy)
+  unsigned int x = tot[d];
+  for (int o = 1; o < 256; o <<= 1) {
+    __syncthreads();
+    const unsigned int y = (d >= o) ? tot[d - o] : 0u;
+    __syncthreads();
+    x += y;
+    tot[d] = x;
+  }
+  __syncthreads();
+  const unsigned int excl = x - run;
+  for (b = 0; b < nblocks; b++) row[b] += excl;
+}
+
+__global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
+    const u64 *__restrict__ kin, const int *__restrict__ vin, u64 *__restrict__ kout,
+    int *__restrict__ vout, int n, int shift, const unsigned int *__restrict__ offs, int nblocks) {
+  __shared__ unsigned int s_base[256];
+  __shared__ unsigned int s_w[kRsThreads / 32][256];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  s_base[tid] = offs[(size_t)tid * nblocks + blockIdx.x];
+  const unsigned int lt = (1u << lane) - 1u;
+  const int base = blockIdx.x * kRsTile;
+  for (int r = 0; r < kRsItems; r++) {
+    const int idx = base + r * kRsThreads + tid;
+    const bool valid = idx < n;
+    const u64 key = valid ? kin[idx] : 0ull;
+    const unsigned int d = valid ? ((unsigned int)(key >> shift) & 255u) : 256u;
+#pragma unroll
+    for (int w = 0; w < kRsThreads / 32; w++) s_w[w][tid] = 0;
+    __syncthreads();
+    const unsigned int peers = __match_any_sync(0xffffffffu, d);
+    const unsigned int rank = __popc(peers & lt);
+    if (valid && rank == 0) s_w[warp][d] = __popc(peers);
+    __syncthreads();
+    {
+      unsigned int run = s_base[tid];
+#pragma unroll
+      for (int w = 0; w < kRsThreads / 32; w++) {
+        const unsigned int c = s_w[w][tid];
+        s_w[w][tid] = run;
+        run += c;
+      }
+      s_base[tid] = run;
+    }
+    __syncthreads();
+    if (valid) {
+      const unsigned int p = s_w[warp][d] + rank;
+      kout[p] = key;
+      vout[p] = vin[idx];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void gather_kernel(const float2 *__restrict__ pos, const int *__restrict__ perm, int n,
+                              float2 *__restrict__ spos) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) spos[k] = pos[perm[k]];
+}
+
+// ---- binary radix tree (Karras 2012) ----------------------------------------
+__device__ __forceinline__ int kdelta(const u64 *__restrict__ K, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  const u64 x = K[i] ^ K[j];
+  return x ? __clzll((long long)x) : 64 + __clz(i ^ j);
+}
+
+// internal node i in [0, n-2]; leaf k encoded as ~k in child links;
+// parent[] holds internal parents of internal nodes (index i) and of leaves
+// (index n-1+k); the root is internal node 0.
+__global__ void radix_tree_kernel(const u64 *__restrict__ K, int n, int2 *child, int2 *range,
+                                  int *dlt, int *parent) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int d = (kdelta(K, n, i, i + 1) - kdelta(K, n, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = kdelta(K, n, i, i - d);
+  int lmax = 2;
+  while (kdelta(K, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t >= 1; t >>= 1)
+    if (kdelta(K, n, i, i + (l + t) * d) > dmin) l += t;
+  const int j = i + l * d;
+  const int dnode = kdelta(K, n, i, j);
+  int s = 0;
+  for (int div = 2;; div <<= 1) {
+    const int t = (l + div - 1) / div;
+    if (kdelta(K, n, i, i + (s + t) * d) > dnode) s += t;
+    if (t <= 1) break;
+  }
+  const int gamma = i + s * d + min(d, 0);
+  const int first = min(i, j), last = max(i, j);
+  const int left = (first == gamma) ? ~gamma : gamma;
+  const int right = (last == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+  child[i] = make_int2(left, right);
+  range[i] = make_int2(first, last);
+  dlt[i] = dnode;
+  parent[left >= 0 ? left : (n - 1 + ~left)] = i;
+  parent[right >= 0 ? right : (n - 1 + ~right)] = i;
+  if (i == 0) parent[0] = -1;
+}
+
+struct TreeArgs {
+  int n;
+  const u64 *keys;
+  const float2 *spos;
+  const int2 *child;
+  const int2 *range;
+  const int *dlt;
+  const int *parent;
+  unsigned int *visit;
+  double2 *qcen;
+  int *qbelow;
+  int *startcnt;
+};
+
+// Internal node merged into its parent's quad node: the x-bit split of the
+// digit whose y-bit split is the parent, or any split inside a run of equal
+// keys below its top.
+__device__ __forceinline__ bool is_sub(const TreeArgs &t, int node) {
+  if (node <= 0) return false;
+  const int p = t.dlt[node];
+  const int pp = t.dlt[t.parent[node]];
+  if (p >= 64) return pp >= 64;
+  return (p & 1) && (pp == p - 1);
+}
+
+__device__ void process_quad(const TreeArgs &t, int node) {
+  const int p = t.dlt[node];
+  const int2 rg = t.range[node];
+  double cx = 0.0, cy = 0.0, cnt = 0.0;
+  int below = 0;
+  if (p >= 64) {
+    // run of identical keys: every point is a child (the reference recurses
+    // without end here; see the oracle's note)
+    for (int k = rg.x; k <= rg.y; k++) {
+      const float2 q = t.spos[k];
+      cx = __dadd_rn(cx, (double)q.x);
+      cy = __dadd_rn(cy, (double)q.y);
+      cnt += 1.0;
+    }
+  } else {
+    int kids[4];
+    int m = 0;
+    const int2 ab = t.child[node];
+    const int sides[2] = {ab.x, ab.y};
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int c = sides[h];
+      if (c >= 0 && is_sub(t, c)) {
+        const int2 cc = t.child[c];
+        kids[m++] = cc.x;
+        kids[m++] = cc.y;
+      } else {
+        kids[m++] = c;
+      }
+    }
+    for (int q = 0; q < m; q++) {
+      const int c = kids[q];
+      double vx, vy;
+      if (c < 0) {
+        const float2 pt = t.spos[~c];
+        vx = (double)pt.x;
+        vy = (double)pt.y;
+      } else {
+        const double2 v = __ldcg(&t.qcen[c]);
+        vx = v.x;
+        vy = v.y;
+        if (q > 0) t.startcnt[__ldcg(&t.range[c].x)] = __ldcg(&t.qbelow[c]) + 1;
+      }
+      cx = __dadd_rn(cx, vx);
+      cy = __dadd_rn(cy, vy);
+      cnt += 1.0;
+    }
+    if (kids[0] >= 0) below = __ldcg(&t.qbelow[kids[0]]) + 1;
+  }
+  cx = __ddiv_rn(cx, cnt);
+  cy = __ddiv_rn(cy, cnt);
+  t.qcen[node] = make_double2(cx, cy);
+  t.qbelow[node] = below;
+  if (node == 0) t.startcnt[rg.x] = below + 1;
+}
+
+__global__ void bottomup_kernel(TreeArgs t) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= t.n) return;
+  int node = t.parent[t.n - 1 + k];
+  // at most one step per tree level: the loop ends at the root (parent -1)
+  // or at the first node this thread reaches before its sibling subtree
+  while (node >= 0) {
+    __threadfence();
+    const unsigned int prev = atomicAdd(&t.visit[node], 1u);
+    if (prev == 0u) return;
+    __threadfence();
+    if (!is_sub(t, node)) process_quad(t, node);
+    node = (node == 0) ? -1 : t.parent[node];
+  }
+}
+
+struct LayoutArgs {
+  int n;
+  DevStatus *st;
+  const float2 *spos;
+  const int2 *range;
+  const int *dlt;
+  const int *parent;
+  const double2 *qcen;
+  const int *qbelow;
+  const int *startcnt;
+  const int *startbase;  // exclusive scan of startcnt, n+1 entries
+  const double *frame;
+  float4 *nodes;
+  double2 *nodes_c64;
+  unsigned char *nodes_lvl;
+};
+
+__global__ void layout_kernel(LayoutArgs L, TreeArgs t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const double maxmin = L.frame[2];
+  const int cap = 2 * L.n - 1;  // records: n leaves + at most n-1 quad nodes
+  if (i < L.n) {  // leaf (sorted point) i
+    const int idx = i + L.startbase[i] + L.startcnt[i];
+    if (idx < 0 || idx >= cap) {
+      dev_record_error(L.st, DEV_BAD_INDEX);
+      return;
+    }
+    const float2 p = L.spos[i];
+    L.nodes[idx] = make_float4(p.x, p.y, 0.0f, __int_as_float(idx + 1));
+    L.nodes_c64[idx] = make_double2((double)p.x, (double)p.y);
+    L.nodes_lvl[idx] = 255;
+  }
+  if (i < L.n - 1 && !is_sub(t, i)) {  // quad node = binary internal node i
+    const int2 rg = L.range[i];
+    const int lo = rg.x, hi = rg.y + 1;
+    const int p = L.dlt[i];
+    const int lvl = p >= 64 ? 32 : (p >> 1);
+    const int rank = L.startcnt[lo] - 1 - L.qbelow[i];
+    const int idx = lo + L.startbase[lo] + rank;
+    const int skip = hi + L.startbase[hi];
+    if (rank < 0 || idx < 0 || idx >= cap || skip <= idx || skip > cap) {
+      dev_record_error(L.st, DEV_BAD_INDEX);
+      return;
+    }
+    const double D = ldexp(maxmin, -lvl);
+    const double2 c = L.qcen[i];
+    L.nodes[idx] = make_float4((float)c.x, (float)c.y, (float)(D * D), __int_as_float(skip));
+    L.nodes_c64[idx] = c;
+    L.nodes_lvl[idx] = (unsigned char)lvl;
+  }
+}
+
+struct TraverseArgs {
+  int n;
+  DevStatus *st;
+  const float4 *nodes;
+  const double2 *nodes_c64;
+  const unsigned char *nodes_lvl;
+  const double *frame;
+  const float2 *spos;
+  const int *perm;
+  float2 *rep;
+  float theta2;
+  double theta;
+  unsigned long long *stats;  // [visits, fp64 decisions] or null
+};
+
+// FP64 opening test exactly as BarnesHut.h:71-72: diameter / distance < theta.
+__device__ __noinline__ bool open_test_fp64(const double2 *__restrict__ c64,
+                                            const unsigned char *__restrict__ lvl,
+                                            const double *__restrict__ frame, double theta,
+                                            int idx, float qx, float qy) {
+  const double2 c = c64[idx];
+  const double D = ldexp(frame[2], -(int)lvl[idx]);
+  const double dx = __dsub_rn(c.x, (double)qx), dy = __dsub_rn(c.y, (double)qy);
+  const double dist = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+  return __ddiv_rn(D, dist) < theta;
+}
+
+__global__ void __launch_bounds__(256) traverse_kernel(TraverseArgs a) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.n) return;
+  const float2 q = a.spos[k];
+  const float qm = fabsf(q.x) + fabsf(q.y);
+  // record 0 is the root; its skip link is the number of records
+  int total = __float_as_int(__ldg(&a.nodes[0]).w);
+  if (total < 0 || total > 2 * a.n - 1) {
+    dev_record_error(a.st, DEV_BAD_INDEX);
+    total = 0;
+  }
+  float fx = 0.f, fy = 0.f;
+  unsigned int visits = 0, exact = 0;
+  int i = 0;
+  while (i < total) {
+    const float4 nd = __ldg(&a.nodes[i]);
+    const float dx = nd.x - q.x, dy = nd.y - q.y;
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
+    const float lhs = a.theta2 * d2;
+    bool accept = nd.z < lhs;
+    if (nd.z > 0.f) {
+      // error bound of the FP32 comparison (centroid rounding, subtraction,
+      // squares, theta^2 and D^2 rounding), with a wide safety factor
+      const float tol = 9.5367432e-07f * (lhs + nd.z) +
+                        a.theta2 * 4.7683716e-07f * (fabsf(dx) + fabsf(dy)) *
+                            (qm + fabsf(nd.x) + fabsf(nd.y));
+      if (fabsf(lhs - nd.z) <= tol) {
+        accept = open_test_fp64(a.nodes_c64, a.nodes_lvl, a.frame, a.theta, i, q.x, q.y);
+        exact++;
+      }
+    }
+    visits++;
+    if (accept) {
+      const float r = rsqrt_approx(d2);
+      fx = fmaf(dx, r, fx);
+      fy = fmaf(dy, r, fy);
+      const int nxt = __float_as_int(nd.w);
+      if (nxt <= i) {  // a skip link always moves forward; stop on a corrupt one
+        dev_record_error(a.st, DEV_BAD_INDEX);
+        break;
+      }
+      i = nxt;
+    } else {
+      i++;
+    }
+  }
+  a.rep[a.perm[k]] = make_float2(fx, fy);
+  if (a.stats) {
+    atomicAdd(&a.stats[0], (unsigned long long)visits);
+    if (exact) atomicAdd(&a.stats[1], (unsigned long long)exact);
+  }
+}
+
+struct SweepArgs {
+  const int *order;
+  int lo, hi, batch;
+  const int *rowptr;
+  const int *colids;
+  const float2 *pold;
+  float2 *pnew;
+  const float2 *rep;
+  double2 *force;
+  double *e;
+  float W;
+  double step;
+};
+
+// Attraction over the CSR row in order (algorithms.cpp:1056-1058), minus the
+// BH repulsion (:1059), then the unit-step update (:1064).
+__global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a) {
+  const int t = a.lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= a.hi) return;
+  const int i = a.order[t];
+  const float2 pi = a.pold[i];
+  const int bi = i / a.batch;
+  double fx = 0.0, fy = 0.0;
+  const int e1 = a.rowptr[i + 1];
+  for (int e = a.rowptr[i]; e < e1; e++) {
+    const int j = a.colids[e];
+    const float2 pj = (j / a.batch < bi) ? __ldcg(&a.pnew[j]) : a.pold[j];
+    const float dx = pj.x - pi.x, dy = pj.y - pi.y;
+    const float s = a.W * sqrtf(fmaf(dx, dx, dy * dy));
+    fx += (double)(dx * s);
+    fy += (double)(dy * s);
+  }
+  const float2 r = a.rep[i];
+  fx -= (double)r.x;
+  fy -= (double)r.y;
+  const double mag = sqrt(fx * fx + fy * fy);
+  float2 np = pi;
+  if (mag > 0.0) {
+    np.x = (float)((double)pi.x + (fx / mag) * a.step);
+    np.y = (float)((double)pi.y + (fy / mag) * a.step);
+  }
+  a.pnew[i] = np;
+  a.force[i] = make_double2(fx, fy);
+  a.e[i] = fx * fx + fy * fy;
+}
+
+inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+int ensure_bh_scratch(bl_ctx *ctx) {
+  const size_t n = (size_t)ctx->g.n;
+  Scratch &s = ctx->s;
+  if (s.bh_n >= n && s.keys) return 0;
+  auto fr = [](void *p) { if (p) cudaFree(p); };
+  fr(s.keys); fr(s.keys_alt); fr(s.perm); fr(s.perm_alt); fr(s.hist); fr(s.spos);
+  fr(s.bparent); fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.visit); fr(s.qcen);
+  fr(s.qbelow); fr(s.startcnt); fr(s.startbase); fr(s.nodes); fr(s.nodes_c64);
+  fr(s.nodes_lvl); fr(s.rep); fr(s.pos_alt);
+  const size_t nb = (n + kRsTile - 1) / kRsTile;
+  s.hist_entries = 256 * std::max<size_t>(nb, 1);
+  const size_t m = std::max<size_t>(n, 2);
+  BL_CUDA(ctx, cudaMalloc(&s.keys, m * 8));
+  BL_CUDA(ctx, cudaMalloc(&s.keys_alt, m * 8));
+  BL_CUDA(ctx, cudaMalloc(&s.perm, m * 4));
+  BL_CUDA(ctx, cudaMalloc(&s.perm_alt, m * 4));
+  BL_CUDA(ctx, cudaMalloc(&s.hist, s.hist_entries * 4));
+  BL_CUDA(ctx, cudaMalloc(&s.spos, m * sizeof(float2)));
+  BL_CUDA(ctx, cudaMalloc(&s.bparent, 2 * m * sizeof(int)));
+  BL_CUDA(ctx, cudaMalloc(&s.bchild, m * sizeof(int2)));
+  BL_CUDA(ctx, cudaMalloc(&s.brange, m * sizeof(int2)));
+  BL_CUDA(ctx, cudaMalloc(&s.bdelta, m * sizeof(int)));
+  BL_CUDA(ctx, cudaMalloc(&s.visit, m * sizeof(unsigned int)));
+  BL_CUDA(ctx, cudaMalloc(&s.qcen, m * sizeof(double2)));
+  BL_CUDA(ctx, cudaMalloc(&s.qbelow, m * sizeof(int)));
+  BL_CUDA(ctx, cudaMalloc(&s.startcnt, (m + 1) * sizeof(int)));
+  BL_CUDA(ctx, cudaMalloc(&s.startbase, (m + 1) * sizeof(int)));
+  BL_CUDA(ctx, cudaMalloc(&s.nodes, 2 * m * sizeof(float4)));
+  BL_CUDA(ctx, cudaMalloc(&s.nodes_c64, 2 * m * sizeof(double2)));
+  BL_CUDA(ctx, cudaMalloc(&s.nodes_lvl, 2 * m));
+  BL_CUDA(ctx, cudaMalloc(&s.rep, m * sizeof(float2)));
+  BL_CUDA(ctx, cudaMalloc(&s.pos_alt, m * sizeof(float2)));
+  s.bh_n = n;
+  return 0;
+}
+
+// Steps 1-4 for the positions `pos`; leaves the pre-order records in
+// ctx->s.nodes (total = n + number of quad nodes, read back by callers that
+// need it via startbase[n]).
+int bh_build(bl_ctx *ctx, const float2 *pos) {
+  const int n = ctx->g.n;
+  Scratch &s = ctx->s;
+  cudaStream_t st = ctx->stream;
+  if (n < 2) return 0;
+  bbox_init_kernel<<<1, 32, 0, st>>>(s.bbox);
+  bbox_kernel<<<std::min(nblk(n, 256), ctx->num_sms * 4), 256, 0, st>>>(pos, n, s.bbox);
+  morton_kernel<<<nblk(n, 256), 256, 0, st>>>(pos, n, s.bbox, s.keys, s.perm, s.frame);
+  ctx->launches += 3;
+  const int nb = nblk(n, kRsTile);
+  unsigned long long *kin = s.keys, *kout = s.keys_alt;
+  int *vin = s.perm, *vout = s.perm_alt;
+  bl_time_begin(ctx, "radix_sort");
+  for (int shift = 0; shift < 64; shift += 8) {
+    rs_hist_kernel<<<nb, kRsThreads, 0, st>>>(kin, n, shift, s.hist, nb);
+    rs_scan_kernel<<<1, 256, 0, st>>>(s.hist, nb);
+    rs_scatter_kernel<<<nb, kRsThreads, 0, st>>>(kin, vin, kout, vout, n, shift, s.hist, nb);
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+    ctx->launches += 3;
+  }
+  bl_time_end(ctx, "radix_sort");
+  // 8 passes: sorted data is back in keys/perm
+  gather_kernel<<<nblk(n, 256), 256, 0, st>>>(pos, s.perm, n, s.spos);
+  radix_tree_kernel<<<nblk(n - 1, 256), 256, 0, st>>>(s.keys, n, s.bchild, s.brange, s.bdelta, s.bparent);
+  BL_CUDA(ctx, cudaMemsetAsync(s.visit, 0, (size_t)n * sizeof(unsigned int), st));
+  BL_CUDA(ctx, cudaMemsetAsync(s.startcnt, 0, (size_t)(n + 1) * sizeof(int), st));
+  TreeArgs t;
+  t.n = n;
+  t.keys = s.keys;
+  t.spos = s.spos;
+  t.child = s.bchild;
+  t.range = s.brange;
+  t.dlt = s.bdelta;
+  t.parent = s.bparent;
+  t.visit = s.visit;
+  t.qcen = s.qcen;
+  t.qbelow = s.qbelow;
+  t.startcnt = s.startcnt;
+  bottomup_kernel<<<nblk(n, 256), 256, 0, st>>>(t);
+  ctx->launches += 3;
+  if (int rc = scan_exclusive_int(ctx, s.startcnt, s.startbase, n + 1)) return rc;
+  LayoutArgs L;
+  L.n = n;
+  L.spos = s.spos;
+  L.range = s.brange;
+  L.dlt = s.bdelta;
+  L.parent = s.bparent;
+  L.qcen = s.qcen;
+  L.qbelow = s.qbelow;
+  L.startcnt = s.startcnt;
+  L.startbase = s.startbase;
+  L.frame = s.frame;
+  L.nodes = s.nodes;
+  L.nodes_c64 = s.nodes_c64;
+  L.nodes_lvl = s.nodes_lvl;
+  L.st = s.status;
+  layout_kernel<<<nblk(n, 256), 256, 0, st>>>(L, t);
+  ctx->launches++;
+  BL_CUDA(ctx, cudaGetLastError());
+  return 0;
+}
+
+int bh_traverse(bl_ctx *ctx, double theta, bool want_stats) {
+  const int n = ctx->g.n;
+  Scratch &s = ctx->s;
+  if (n < 2) {
+    BL_CUDA(ctx, cudaMemsetAsync(s.rep, 0, sizeof(float2) * std::max(n, 1), ctx->stream));
+    return 0;
+  }
+  TraverseArgs a;
+  a.n = n;
+  a.nodes = s.nodes;
+  a.nodes_c64 = s.nodes_c64;
+  a.nodes_lvl = s.nodes_lvl;
+  a.frame = s.frame;
+  a.spos = s.spos;
+  a.perm = s.perm;
+  a.rep = s.rep;
+  a.theta = theta;
+  a.theta2 = (float)(theta * theta);
+  a.stats = want_stats ? s.stats : nullptr;
+  a.st = s.status;
+  if (want_stats) BL_CUDA(ctx, cudaMemsetAsync(s.stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
+  bl_time_begin(ctx, "traverse_kernel");
+  traverse_kernel<<<nblk(n, 256), 256, 0, ctx->stream>>>(a);
+  bl_time_end(ctx, "traverse_kernel");
+  ctx->launches++;
+  BL_CUDA(ctx, cudaGetLastError());
+  return 0;
+}
+
+int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_energy,
+                 double *energy_out) {
+  if (int rc = ensure_bh_scratch(ctx)) return rc;
+  const LevelSchedule *ls = level_schedule(ctx, batch);
+  if (!ls) return -2;
+  float2 *pold = ctx->pos, *pnew = ctx->s.pos_alt;
+  if (int rc = bh_build(ctx, pold)) return rc;
+  if (int rc = bh_traverse(ctx, theta, false)) return rc;
+  SweepArgs a;
+  a.order = ls->order;
+  a.batch = batch;
+  a.rowptr = ctx->g.rowptr;
+  a.colids = ctx->g.colids;
+  a.pold = pold;
+  a.pnew = pnew;
+  a.rep = ctx->s.rep;
+  a.force = ctx->force;
+  a.e = ctx->e;
+  a.W = (float)ctx->weight;
+  a.step = step;
+  bl_time_begin(ctx, "sweep_kernel");
+  for (int l = 0; l < ls->levels; l++) {
+    a.lo = ls->offsets[l];
+    a.hi = ls->offsets[l + 1];
+    if (a.hi <= a.lo) continue;
+    sweep_kernel<<<nblk(a.hi - a.lo, 256), 256, 0, ctx->stream>>>(a);
+    ctx->launches++;
+  }
+  bl_time_end(ctx, "sweep_kernel");
+  BL_CUDA(ctx, cudaGetLastError());
+  std::swap(ctx->pos, ctx->s.pos_alt);
+  if (want_energy) {
+    if (int rc = energy_reduce(ctx, energy_out)) return rc;
+    return bl_check_status(ctx);
+  }
+  return 0;
+}
+
+int bh_canonical_tree(bl_ctx *ctx, int cap, int *lo, int *hi, int *depth, int *nchild,
+                      double *centroid) {
+  const int n = ctx->g.n;
+  if (n < 2) return 0;
+  if (int rc = ensure_bh_scratch(ctx)) return rc;
+  if (n < 2) return 0;
+  if (int rc = bh_build(ctx, ctx->pos)) return rc;
+  // copy the binary tree back and emit quad nodes in pre-order (host walk)
+  std::vector<int2> child(n - 1), range(n - 1);
+  std::vector<int> dlt(n - 1), parent(2 * n - 1);
+  std::vector<double2> qcen(n - 1);
+  cudaStream_t st = ctx->stream;
+  BL_CUDA(ctx, cudaMemcpyAsync(child.data(), ctx->s.bchild, (n - 1) * sizeof(int2), cudaMemcpyDeviceToHost, st));
+  BL_CUDA(ctx, cudaMemcpyAsync(range.data(), ctx->s.brange, (n - 1) * sizeof(int2), cudaMemcpyDeviceToHost, st));
+  BL_CUDA(ctx, cudaMemcpyAsync(dlt.data(), ctx->s.bdelta, (n - 1) * sizeof(int), cudaMemcpyDeviceToHost, st));
+  BL_CUDA(ctx, cudaMemcpyAsync(parent.data(), ctx->s.bparent, (2 * n - 1) * sizeof(int), cudaMemcpyDeviceToHost, st));
+  BL_CUDA(ctx, cudaMemcpyAsync(qcen.data(), ctx->s.qcen, (n - 1) * sizeof(double2), cudaMemcpyDeviceToHost, st));
+  BL_CUDA(ctx, cudaStreamSynchronize(st));
+  if (int rc = bl_check_status(ctx)) return rc;
+  auto sub = [&](int node) {
+    if (node <= 0) return false;
+    const int p = dlt[node], pp = dlt[parent[node]];
+    if (p >= 64) return pp >= 64;
+    return (p & 1) && pp == p - 1;
+  };
+  int count = 0;
+  std::vector<int> stack{0};
+  while (!stack.empty()) {
+    const int v = stack.back();
+    stack.pop_back();
+    std::vector<int> kids;
+    if (dlt[v] >= 64) {
+      kids.clear();
+    } else {
+      const int sides[2] = {child[v].x, child[v].y};
+      for (int c : sides) {
+        if (c >= 0 && sub(c)) {
+          kids.push_back(child[c].x);
+          kids.push_back(child[c].y);
+        } else {
+          kids.push_back(c);
+        }
+      }
+    }
+    if (count < cap) {
+      lo[count] = range[v].x;
+      hi[count] = range[v].y + 1;
+      depth[count] = dlt[v] >= 64 ? 32 : dlt[v] / 2;
+      nchild[count] = dlt[v] >= 64 ? (range[v].y - range[v].x + 1) : (int)kids.size();
+      centroid[2 * count] = qcen[v].x;
+      centroid[2 * count + 1] = qcen[v].y;
+    }
+    count++;
+    for (int q = (int)kids.size() - 1; q >= 0; q--)
+      if (kids[q] >= 0) stack.push_back(kids[q]);
+  }
+  return count;
+}
+
+// Dependency levels of the attraction sweep for batch size `batch`:
+// level(i) = 0 without neighbours in earlier batches, else 1 + the largest
+// level among them.  Cached per batch size.
+const LevelSchedule *level_schedule(bl_ctx *ctx, int batch) {
+  for (auto &ls : ctx->schedules)
+    if (ls.batch == batch) return &ls;
+  const int n = ctx->g.n;
+  const std::vector<int> &rp = ctx->h_rowptr, &ci = ctx->h_colids;
+  std::vector<int> lev(n, 0);
+  int maxl = 0;
+  for (int i = 0; i < n; i++) {
+    const int bi = i / batch;
+    int l = -1;
+    for (int e = rp[i]; e < rp[i + 1]; e++) {
+      const int j = ci[e];
+      if (j / batch < bi) l = std::max(l, lev[j]);
+    }
+    lev[i] = l + 1;
+    maxl = std::max(maxl, l + 1);
+  }
+  LevelSchedule ls;
+  ls.batch = batch;
+  ls.levels = n > 0 ? maxl + 1 : 0;
+  ls.offsets.assign(ls.levels + 1, 0);
+  for (int i = 0; i < n; i++) ls.offsets[lev[i] + 1]++;
+  for (int l = 0; l < ls.levels; l++) ls.offsets[l + 1] += ls.offsets[l];
+  std::vector<int> order(std::max(n, 1));
+  std::vector<int> fill(ls.offsets.begin(), ls.offsets.end() - 1);
+  for (int i = 0; i < n; i++) order[fill[lev[i]]++] = i;
+  if (cudaMalloc(&ls.order, order.size() * sizeof(int)) != cudaSuccess) {
+    bl_fail(ctx, -2, "cudaMalloc level schedule");
+    return nullptr;
+  }
+  if (cudaMemcpy(ls.order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+    bl_fail(ctx, -2, "cudaMemcpy level schedule");
+    return nullptr;
+  }
+  ctx->schedules.push_back(std::move(ls));
+  return &ctx->schedules.back();
+}
+
+}  // namespace bl

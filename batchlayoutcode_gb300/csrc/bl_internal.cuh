@@ -1,0 +1,228 @@
+// bl_internal.cuh -- shared declarations of the GB300 BatchLayout engine.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <deque>
+#include <string>
+#include <vector>
+
+// ----------------------------------------------------------------------------
+// Device-side error record.  Every spin-wait in this library is bounded; when
+// a bound runs out the waiting block records the site here and returns, the
+// host reads the record after the kernel and reports BL_ERR_DEVICE_TIMEOUT.
+// ----------------------------------------------------------------------------
+enum : unsigned int {
+  DEV_OK = 0,
+  DEV_TIMEOUT_GRID_BARRIER = 1,
+  DEV_TIMEOUT_TREE = 2,
+  DEV_BAD_INDEX = 3,
+};
+
+struct DevStatus {
+  unsigned int code;     // first error code (0 = none)
+  unsigned int where;    // block id that recorded it
+  unsigned int barrier;  // grid-barrier generation counter
+  unsigned int pad;
+};
+
+// Timeouts for device waits (nanoseconds of %globaltimer).
+constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ unsigned long long dev_globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ unsigned int ld_volatile_u32(const unsigned int *p) {
+  return *reinterpret_cast<const volatile unsigned int *>(p);
+}
+
+__device__ __forceinline__ void dev_record_error(DevStatus *st, unsigned int code) {
+  if (atomicCAS(&st->code, 0u, code) == 0u) st->where = blockIdx.x;
+}
+
+// Grid-wide barrier for a cooperative (co-resident) launch.  `epoch` counts
+// the barriers this block has passed; the counter is monotone within one
+// launch and reset by the host before it.  Returns false when the grid must
+// stop (timeout here or an error recorded elsewhere).
+__device__ __forceinline__ bool grid_barrier(DevStatus *st, unsigned int &epoch) {
+  __syncthreads();
+  epoch++;
+  __shared__ unsigned int s_ok;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(&st->barrier, 1u);
+    const unsigned int target = epoch * gridDim.x;
+    const unsigned long long t0 = dev_globaltimer();
+    unsigned int ok = 1;
+    while (ld_acquire_gpu(&st->barrier) < target) {
+      if (ld_volatile_u32(&st->code) != 0u) {
+        ok = 0;
+        break;
+      }
+      if (dev_globaltimer() - t0 > kBarrierTimeoutNs) {
+        dev_record_error(st, DEV_TIMEOUT_GRID_BARRIER);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    if (ld_volatile_u32(&st->code) != 0u) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// Added to every squared distance in FP32: leaves |d|^2 >= ~1e-23 bit-identical
+// and turns the coincident case (d = 0) into a zero contribution 0 * (1/tiny)
+// instead of 0 * inf, which is what the reference's `dist > 0` guard yields.
+constexpr float kTinyD2 = 1e-30f;
+
+// ----------------------------------------------------------------------------
+// Host-side helpers
+// ----------------------------------------------------------------------------
+struct KernelTimer;  // per-kernel CUDA-event timing (api.cu)
+
+namespace bl {
+
+// Force models of the minibatch sweep (sample/algorithms.cpp:759, :912, :985).
+enum Model { MODEL_FR = 2, MODEL_LINLOG = 3, MODEL_FA = 8 };
+
+struct DeviceGraph {
+  int n = 0;
+  long long nnz = 0;
+  int *rowptr = nullptr;      // CSR of the graph
+  int *colids = nullptr;
+  int *eff_rowptr = nullptr;  // neighbours the minibatch cursor actually matches
+  int *eff_colids = nullptr;
+  int max_eff_degree = 0;
+};
+
+// Level schedule of the Barnes-Hut attraction sweep for one batch size.
+struct LevelSchedule {
+  int batch = 0;
+  int levels = 0;
+  std::vector<int> offsets;  // host copy, levels + 1 entries
+  int *order = nullptr;      // device: vertices grouped by level
+};
+
+struct Scratch {
+  // generic
+  double *energy_parts = nullptr;  // per-block energy partials
+  double *energy = nullptr;        // per-iteration energies (device)
+  DevStatus *status = nullptr;
+  // minibatch sweep
+  float2 *partials = nullptr;
+  size_t partials_bytes = 0;
+  // Barnes-Hut
+  size_t bh_n = 0;
+  unsigned long long *keys = nullptr, *keys_alt = nullptr;
+  int *perm = nullptr, *perm_alt = nullptr;
+  unsigned int *hist = nullptr;  // radix histograms / offsets
+  size_t hist_entries = 0;
+  unsigned int *bbox = nullptr;  // 4 ordered-uint encoded floats
+  double *frame = nullptr;       // minX, minY, MAXMIN
+  float2 *spos = nullptr;        // positions in Morton order
+  int *bparent = nullptr;        // binary radix tree: parent of node (internal i, leaf n-1+k)
+  int2 *bchild = nullptr;        // children of internal node (encoded: >= 0 internal, < 0 leaf ~k)
+  int2 *brange = nullptr;        // [first, last] of internal node
+  int *bdelta = nullptr;         // common prefix length of internal node
+  unsigned int *visit = nullptr; // bottom-up arrival counters
+  double2 *qcen = nullptr;       // centroid of quad node (indexed by binary internal id)
+  int *qbelow = nullptr;         // chain length below a quad node
+  int *startcnt = nullptr;       // quad nodes starting at each sorted position (n+1)
+  int *startbase = nullptr;      // exclusive scan of startcnt (n+1)
+  int *scan_tmp = nullptr;
+  float4 *nodes = nullptr;       // pre-order records {x, y, D^2, skip}
+  double2 *nodes_c64 = nullptr;  // FP64 centroid per pre-order record
+  unsigned char *nodes_lvl = nullptr;
+  float2 *rep = nullptr;         // BH repulsion per vertex
+  unsigned long long *stats = nullptr;
+  float2 *pos_alt = nullptr;     // second position buffer (Gauss-Seidel sweep)
+};
+
+}  // namespace bl
+
+struct bl_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // run options (reference constructor arguments)
+  std::string input, outputdir, initfile;
+  int init = 0;
+  double weight = 1.0, threshold = 0.01;
+  // graph
+  bl::DeviceGraph g;
+  std::vector<int> h_rowptr, h_colids;
+  // layout state
+  float2 *pos = nullptr;      // current coordinates (float32)
+  double2 *force = nullptr;   // forces of the last iteration
+  double *e = nullptr;        // |f|^2 per vertex
+  double2 *stage = nullptr;   // FP64 staging for coordinate transfers
+  bl::Scratch s;
+  std::deque<bl::LevelSchedule> schedules;  // stable addresses
+  long long launches = 0;
+  bool graph_mode = false;
+  // timing of one kernel family for the roofline
+  std::string timed_kernel;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  double timed_ms = 0.0;
+  long long timed_count = 0;
+  cudaEvent_t run_ev[2] = {nullptr, nullptr};
+  double last_run_ms = 0.0;
+};
+
+// ---- helpers implemented in api.cu ---------------------------------------
+int bl_fail(bl_ctx *ctx, int code, const std::string &msg);
+int bl_cuda_fail(bl_ctx *ctx, cudaError_t e, const char *what);
+int bl_check_status(bl_ctx *ctx);
+void bl_time_begin(bl_ctx *ctx, const char *kernel);
+void bl_time_end(bl_ctx *ctx, const char *kernel);
+
+#define BL_CUDA(ctx, call)                                  \
+  do {                                                      \
+    cudaError_t _e = (call);                                \
+    if (_e != cudaSuccess) return bl_cuda_fail(ctx, _e, #call); \
+  } while (0)
+
+// ---- kernels drivers (smu.cu, bh.cu, reduce.cu) ----------------------------
+namespace bl {
+int ensure_minibatch_scratch(bl_ctx *ctx, int batch, int grid);
+int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step0,
+                  double decay, bool converged, double engt, long long max_loops,
+                  double *energy_out, long long *loops_out);
+int ensure_bh_scratch(bl_ctx *ctx);
+int bh_build(bl_ctx *ctx, const float2 *pos);
+int bh_traverse(bl_ctx *ctx, double theta, bool want_stats);
+int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_energy,
+                 double *energy_out);
+int bh_canonical_tree(bl_ctx *ctx, int cap, int *lo, int *hi, int *depth, int *nchild,
+                      double *centroid);
+const LevelSchedule *level_schedule(bl_ctx *ctx, int batch);
+int energy_reduce(bl_ctx *ctx, double *out_host);
+int scan_exclusive_int(bl_ctx *ctx, const int *in, int *out, int n);
+}  // namespace bl

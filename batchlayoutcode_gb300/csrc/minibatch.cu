@@ -1,0 +1,366 @@
+// minibatch.cu -- all-pairs stochastic minibatch update (algo 2 / 3 / 8).
+//
+// Reference: sample/algorithms.cpp:739-783 (FR), :894-936 (LinLog),
+// :967-1009 (FA).  Vertices are processed in consecutive batches of `batch`
+// ids; every force of a batch uses the positions at the start of that batch
+// (Jacobi inside a batch) and the batch then moves by STEP * f/|f| before the
+// next batch starts (Gauss-Seidel across batches).  f_i is attraction over
+// the neighbours matched by the sorted-CSR cursor (kindex, :758-762) plus
+// repulsion -d/|d|^2 over every other vertex with |d| > 0.
+//
+// GB300 design: one persistent cooperative kernel runs every iteration and
+// batch.  Each block owns a contiguous slice of source vertices kept in shared
+// memory for the whole run (8 B per vertex, float2).  For batch c every block
+// sweeps its slice against the batch's targets with a branch-free inner loop
+// (repulsion for all pairs; 7 FP32 instructions per pair, one MUFU rcp), and
+// writes one FP32 partial force per target.  After a grid barrier the block(s)
+// whose slice holds batch c sum the partials in FP64 in a fixed order, correct
+// the neighbour pairs (remove their repulsion, add the model's attraction --
+// the decomposition the reference's own algo 7 uses, :553-579), move the
+// vertices and refresh their shared-memory copy.  Blocks that do not own
+// batch c go straight on to batch c+1: the only values that changed are batch
+// c's own positions, which live in the owners' slices.
+//
+// Algorithmic work: 10 flops per ordered pair (2 sub, 3 for |d|^2, 1 rcp,
+// 2 FMA x 2 components counted as 4), n*n pairs per iteration.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+
+#include "bl_internal.cuh"
+
+namespace bl {
+namespace {
+
+constexpr int kThreads = 512;
+constexpr int kGroups = 4;                     // source sub-slices per block
+constexpr int kGroup = kThreads / kGroups;     // 128 threads per group
+constexpr int kChunk = 2 * kGroup;             // 256 targets per sweep pass
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxBatch = 4096;
+
+struct MinibatchArgs {
+  int n, batch, nbatches, model, grid;
+  double W;
+  const int *eff_rowptr, *eff_colids;
+  float2 *pos;
+  double2 *force;
+  double *e;
+  float2 *partials;       // [2][batch][grid]
+  double *energy;         // energy per iteration (device)
+  double *energy_parts;   // [grid]
+  long long *loops;       // iterations run (device, 1 value)
+  DevStatus *st;
+  int iterations;
+  double step0, decay;
+  int converged;
+  double engt;
+  long long max_loops;
+};
+
+__device__ __forceinline__ void rep_pair(float xs, float ys, float xi, float yi, float &fx,
+                                         float &fy) {
+  const float dx = xs - xi, dy = ys - yi;
+  const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
+  const float r = rcp_approx(d2);
+  fx = fmaf(-dx, r, fx);
+  fy = fmaf(-dy, r, fy);
+}
+
+// Slice of sources owned by block s: [lo, hi).
+__device__ __forceinline__ void slice_of(int n, int grid, int s, int &lo, int &hi) {
+  lo = (int)(((long long)n * s) / grid);
+  hi = (int)(((long long)n * (s + 1)) / grid);
+}
+
+__device__ double block_sum(double v, double *red) {
+  // fixed-order tree: warp xor-shuffle, then warp 0 over the warp sums
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (w == 0) {
+    t = (l < kWarps) ? red[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int s = blockIdx.x;
+  int slo, shi;
+  slice_of(a.n, a.grid, s, slo, shi);
+  const int sbase = slo & ~1;  // even so that pairs of sources load as float4
+  const int slen = shi - sbase;
+  float2 *slice = reinterpret_cast<float2 *>(smem_raw);
+  const int slen_pad = (slen + 3) & ~3;
+  float2 *gsum = slice + slen_pad;              // [kGroups-1][kChunk]
+  float2 *tpos = gsum + (kGroups - 1) * kChunk;  // [batch]
+  __shared__ double red[kWarps];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int grp = tid / kGroup, gl = tid % kGroup;
+
+  for (int k = tid; k < slen; k += kThreads) slice[k] = a.pos[sbase + k];
+  // group sub-ranges of [slo, shi) in slice-local indices
+  const int la = slo - sbase, lb = shi - sbase;
+  const int ga = la + (int)((long long)(lb - la) * grp / kGroups);
+  const int gb = la + (int)((long long)(lb - la) * (grp + 1) / kGroups);
+  __syncthreads();
+
+  unsigned int epoch = 0;
+  double step = a.step0;
+  double e_prev = DBL_MAX, e_cur = 0.0;
+  long long loop = 0;
+  bool ok = true;
+
+  while (ok) {
+    if (a.converged) {
+      if (!(fabs(e_prev - e_cur) / e_prev > a.engt) || loop >= a.max_loops) break;
+    } else if (loop >= a.iterations) {
+      break;
+    }
+    const bool need_energy = a.converged || (loop == a.iterations - 1);
+    for (int c = 0; c < a.nbatches && ok; c++) {
+      const int base = c * a.batch;
+      const int cnt = min(a.batch, a.n - base);
+      const int buf = c & 1;
+      for (int t = tid; t < cnt; t += kThreads) tpos[t] = a.pos[base + t];
+      __syncthreads();
+      // ---- sweep: partial repulsion of this block's slice on every target ----
+      for (int c0 = 0; c0 < cnt; c0 += kChunk) {
+        const int t0 = c0 + gl, t1 = t0 + kGroup;
+        const float2 p0 = (t0 < cnt) ? tpos[t0] : make_float2(0.f, 0.f);
+        const float2 p1 = (t1 < cnt) ? tpos[t1] : make_float2(0.f, 0.f);
+        float fx0a = 0.f, fy0a = 0.f, fx0b = 0.f, fy0b = 0.f;
+        float fx1a = 0.f, fy1a = 0.f, fx1b = 0.f, fy1b = 0.f;
+        int k = ga;
+        if ((k & 1) && k < gb) {
+          const float2 q = slice[k];
+          rep_pair(q.x, q.y, p0.x, p0.y, fx0a, fy0a);
+          rep_pair(q.x, q.y, p1.x, p1.y, fx1a, fy1a);
+          k++;
+        }
+#pragma unroll 4
+        for (; k + 1 < gb; k += 2) {
+          const float4 q = *reinterpret_cast<const float4 *>(&slice[k]);
+          rep_pair(q.x, q.y, p0.x, p0.y, fx0a, fy0a);
+          rep_pair(q.z, q.w, p0.x, p0.y, fx0b, fy0b);
+          rep_pair(q.x, q.y, p1.x, p1.y, fx1a, fy1a);
+          rep_pair(q.z, q.w, p1.x, p1.y, fx1b, fy1b);
+        }
+        if (k < gb) {
+          const float2 q = slice[k];
+          rep_pair(q.x, q.y, p0.x, p0.y, fx0b, fy0b);
+          rep_pair(q.x, q.y, p1.x, p1.y, fx1b, fy1b);
+        }
+        const float2 r0 = make_float2(fx0a + fx0b, fy0a + fy0b);
+        const float2 r1 = make_float2(fx1a + fx1b, fy1a + fy1b);
+        if (grp > 0) {
+          gsum[(grp - 1) * kChunk + gl] = r0;
+          gsum[(grp - 1) * kChunk + gl + kGroup] = r1;
+        }
+        __syncthreads();
+        if (grp == 0) {
+          float2 o0 = r0, o1 = r1;
+#pragma unroll
+          for (int g = 0; g < kGroups - 1; g++) {
+            const float2 u0 = gsum[g * kChunk + gl], u1 = gsum[g * kChunk + gl + kGroup];
+            o0.x += u0.x; o0.y += u0.y;
+            o1.x += u1.x; o1.y += u1.y;
+          }
+          float2 *P = a.partials + (size_t)buf * a.batch * a.grid;
+          if (t0 < cnt) P[(size_t)t0 * a.grid + s] = o0;
+          if (t1 < cnt) P[(size_t)t1 * a.grid + s] = o1;
+        }
+        __syncthreads();
+      }
+      ok = grid_barrier(a.st, epoch);
+      if (!ok) break;
+      // ---- owners: reduce partials, neighbour correction, update ------------
+      const int olo = max(slo, base), ohi = min(shi, base + cnt);
+      if (olo < ohi) {
+        const float2 *P = a.partials + (size_t)buf * a.batch * a.grid;
+        for (int i = olo + warp; i < ohi; i += kWarps) {
+          const int t = i - base;
+          double fx = 0.0, fy = 0.0;
+          for (int q = lane; q < a.grid; q += 32) {
+            const float2 v = __ldcg(&P[(size_t)t * a.grid + q]);
+            fx += (double)v.x;
+            fy += (double)v.y;
+          }
+          const float2 pi = tpos[t];
+          double cx = 0.0, cy = 0.0;
+          const int k0 = a.eff_rowptr[i], k1 = a.eff_rowptr[i + 1];
+          for (int k = k0 + lane; k < k1; k += 32) {
+            const int j = a.eff_colids[k];
+            const float2 pj = (j >= base && j < base + cnt) ? tpos[j - base] : __ldcg(&a.pos[j]);
+            const float dx = pj.x - pi.x, dy = pj.y - pi.y;
+            // the sweep added -d/|d|^2 for this pair: take it back
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
+            const float r = rcp_approx(d2);
+            float ax, ay;
+            if (a.model == MODEL_FR) {
+              const float sc = (float)a.W * sqrtf(dx * dx + dy * dy);
+              ax = dx * sc; ay = dy * sc;
+            } else if (a.model == MODEL_LINLOG) {
+              const float sc = log2f(1.0f + (float)a.W * sqrtf(dx * dx + dy * dy));
+              ax = dx * sc; ay = dy * sc;
+            } else {
+              ax = dx * (float)a.W; ay = dy * (float)a.W;
+            }
+            cx += (double)ax + (double)(dx * r);
+            cy += (double)ay + (double)(dy * r);
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            fx += __shfl_xor_sync(0xffffffffu, fx, o);
+            fy += __shfl_xor_sync(0xffffffffu, fy, o);
+            cx += __shfl_xor_sync(0xffffffffu, cx, o);
+            cy += __shfl_xor_sync(0xffffffffu, cy, o);
+          }
+          if (lane == 0) {
+            fx += cx;
+            fy += cy;
+            const double mag = sqrt(fx * fx + fy * fy);
+            float2 np = pi;
+            if (mag > 0.0) {
+              np.x = (float)((double)pi.x + (fx / mag) * step);
+              np.y = (float)((double)pi.y + (fy / mag) * step);
+            }
+            a.pos[i] = np;
+            slice[i - sbase] = np;
+            a.force[i] = make_double2(fx, fy);
+            a.e[i] = fx * fx + fy * fy;
+          }
+        }
+      }
+      // owner warps still read tpos and write the slice: finish before the
+      // next batch reloads tpos and sweeps the slice
+      __syncthreads();
+    }
+    if (!ok) break;
+    if (need_energy) {
+      ok = grid_barrier(a.st, epoch);
+      if (!ok) break;
+      double v = 0.0;
+      for (int i = slo + tid; i < shi; i += kThreads) v += __ldcg(&a.e[i]);
+      v = block_sum(v, red);
+      if (tid == 0) a.energy_parts[s] = v;
+      ok = grid_barrier(a.st, epoch);
+      if (!ok) break;
+      double tot = 0.0;
+      if (tid == 0)
+        for (int q = 0; q < a.grid; q++) tot += __ldcg(&a.energy_parts[q]);
+      if (tid == 0) red[0] = tot;
+      __syncthreads();
+      tot = red[0];
+      __syncthreads();
+      e_prev = e_cur;
+      e_cur = tot;
+      if (s == 0 && tid == 0) a.energy[0] = tot;
+    }
+    step = step * a.decay;
+    loop++;
+  }
+  if (s == 0 && tid == 0) *a.loops = loop;
+}
+
+}  // namespace
+
+int ensure_minibatch_scratch(bl_ctx *ctx, int batch, int grid) {
+  const size_t need = (size_t)2 * batch * grid * sizeof(float2);
+  if (ctx->s.partials_bytes < need) {
+    if (ctx->s.partials) cudaFree(ctx->s.partials);
+    ctx->s.partials = nullptr;
+    ctx->s.partials_bytes = 0;
+    BL_CUDA(ctx, cudaMalloc(&ctx->s.partials, need));
+    ctx->s.partials_bytes = need;
+  }
+  return 0;
+}
+
+int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step0,
+                  double decay, bool converged, double engt, long long max_loops,
+                  double *energy_out, long long *loops_out) {
+  const int n = ctx->g.n;
+  if (batch < 1) return bl_fail(ctx, -1, "batch must be >= 1");
+  if (n < 1) return bl_fail(ctx, -7, "no graph loaded");
+  batch = std::min(batch, n);  // a batch larger than n is one Jacobi batch
+  if (batch > kMaxBatch)
+    return bl_fail(ctx, -5, "minibatch path supports batch <= 4096 (got " + std::to_string(batch) + ")");
+  if (!converged && iterations <= 0) {
+    if (energy_out) *energy_out = 0.0;
+    if (loops_out) *loops_out = 0;
+    return 0;
+  }
+  int grid = std::min(ctx->num_sms, std::max(1, (n + 127) / 128));
+  int dev_smem_optin = 0;
+  cudaDeviceGetAttribute(&dev_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+  auto smem_for = [&](int g) {
+    const int slice_max = (n + g - 1) / g + 2;
+    return (size_t)(((slice_max + 3) & ~3) + (kGroups - 1) * kChunk + batch) * sizeof(float2);
+  };
+  while (smem_for(grid) + 1024 > (size_t)dev_smem_optin && grid < ctx->num_sms) grid++;
+  const size_t smem = smem_for(grid);
+  if (smem + 1024 > (size_t)dev_smem_optin)
+    return bl_fail(ctx, -5, "graph too large for the shared-memory source slices of the minibatch path");
+  BL_CUDA(ctx, cudaFuncSetAttribute(minibatch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0;
+  BL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, minibatch_kernel, kThreads, smem));
+  if (occ < 1 || grid > occ * ctx->num_sms)
+    return bl_fail(ctx, -5, "minibatch kernel cannot be co-resident");
+  if (int rc = ensure_minibatch_scratch(ctx, batch, grid)) return rc;
+  BL_CUDA(ctx, cudaMemsetAsync(ctx->s.status, 0, sizeof(DevStatus), ctx->stream));
+
+  MinibatchArgs a;
+  a.n = n;
+  a.batch = batch;
+  a.nbatches = (n + batch - 1) / batch;
+  a.model = model;
+  a.grid = grid;
+  a.W = ctx->weight;
+  a.eff_rowptr = ctx->g.eff_rowptr;
+  a.eff_colids = ctx->g.eff_colids;
+  a.pos = ctx->pos;
+  a.force = ctx->force;
+  a.e = ctx->e;
+  a.partials = ctx->s.partials;
+  a.energy = ctx->s.energy;
+  a.energy_parts = ctx->s.energy_parts;
+  a.loops = reinterpret_cast<long long *>(ctx->s.energy + 1);
+  a.st = ctx->s.status;
+  a.iterations = iterations;
+  a.step0 = step0;
+  a.decay = decay;
+  a.converged = converged ? 1 : 0;
+  a.engt = engt;
+  a.max_loops = max_loops;
+  void *args[] = {&a};
+  bl_time_begin(ctx, "minibatch_kernel");
+  BL_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)minibatch_kernel, dim3(grid), dim3(kThreads),
+                                           args, smem, ctx->stream));
+  bl_time_end(ctx, "minibatch_kernel");
+  ctx->launches++;
+  double host[2];
+  BL_CUDA(ctx, cudaMemcpyAsync(host, ctx->s.energy, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (int rc = bl_check_status(ctx)) return rc;
+  long long loops;
+  memcpy(&loops, &host[1], sizeof(loops));
+  if (energy_out) *energy_out = host[0];
+  if (loops_out) *loops_out = loops;
+  return 0;
+}
+
+}  // namespace bl

@@ -1,0 +1,347 @@
+#!/usr/bin/env python3
+"""Barnes-Hut layout throughput (vertex-iterations/s) on one GB300.
+
+Workload (default): random geometric graph, 1,000,000 points uniform in the
+unit square, mean degree 6, largest connected component (986,822 vertices,
+2,977,701 edges), uniform init in [-3,3]^2, algo 4 (BarnesHutApproximation),
+bht 1.2, batch 256.  One step = one iteration of the layout over the whole
+graph (tree build, repulsion of every vertex, attraction + minibatch updates).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+value      device-resident throughput: n * K / (sum of CUDA-event times of the
+           K steps); L2 flushed (256 MB write) before every timed step.
+e2e        the same through the C ABI with host buffers: per step, copy the
+           coordinates from pinned host memory, run the iteration, copy them
+           back (host wall clock).
+roofline   dominant kernel (the repulsion traversal): algorithmic bytes =
+           node-record visits x 16 B per launch, over its CUDA-event time.
+cpu_baseline  the FP64 oracle port (reference Makefile optimisation flags)
+           on all host cores, a bounded sample of iterations from the same start.
+
+With --impl reference the reference's CPU implementation is timed on the same
+workload (oracle/_ref/BatchLayout when it exists and runs here, else the port).
+Multi-GPU: independent replicas (the layout has no data-parallel split that
+avoids a per-batch all-gather), one per rank, value = sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "1M-vertex BH layout: s to plain-energy (learned vs plain), vertex-iters/s"
+UNIT = "vertex-iters/s"
+WORKLOADS = {
+    "rgg1m": dict(algo=4, batch=256, theta=1.2,
+                  desc="random geometric graph, 1,000,000 points in the unit square, mean degree 6, "
+                       "largest component; uniform init in [-3,3]^2; algo 4 (Barnes-Hut), bht 1.2, batch 256"),
+    "chunglu100k": dict(algo=2, batch=256, theta=1.2,
+                        desc="Chung-Lu power-law graph, 100,000 vertices, exponent 2.5, mean degree 10, "
+                             "largest component; disc init; algo 2 (all-pairs minibatch), batch 256"),
+    "grid64": dict(algo=2, batch=256, theta=1.2,
+                   desc="64x64 triangulated grid (4,096 vertices, 12,033 edges); disc init; algo 2, batch 256"),
+}
+KERNEL_FOR_ALGO = {4: "traverse_kernel", 2: "minibatch_kernel", 3: "minibatch_kernel", 8: "minibatch_kernel"}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(k)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        return None
+
+
+def traffic_from_profile(kernel: str, workload: str):
+    """dram bytes per launch from the committed ncu summary, if there is one."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+def load_workload(name: str):
+    from batchlayoutcode_gb300 import graphs as G
+    return G.cached_workload(name)
+
+
+def cpu_baseline_port(g, xy, w, iters: int, threads: int | None = None):
+    import oracle
+    t0 = time.perf_counter()
+    _, e, loops = oracle.layout(w["algo"], g.rowptr, g.colids, xy.astype("float64"), iters, w["batch"],
+                                w["theta"], nthreads=threads, fast=True)
+    dt = time.perf_counter() - t0
+    return g.n * iters / dt, dt
+
+
+def baseline_iters(w, n):
+    # about 10-30 s of CPU work on a 16-core host
+    if w["algo"] == 4:
+        return max(2, min(50, int(2.0e7 / max(n, 1))))
+    return max(1, min(600, int(2.0e11 / max(n * n, 1))))
+
+
+def run_reference(args, w, g, xy):
+    """Reference CPU implementation on the same workload."""
+    cores = os.cpu_count() or 1
+    ref_bin = os.path.join(ROOT, "oracle", "_ref", "BatchLayout")
+    steps = args.steps + args.warmup
+    iters_per_step = 1
+    kind = "port"
+    sample = None
+    value = None
+    if os.path.exists(ref_bin) and os.access(ref_bin, os.X_OK):
+        try:
+            from batchlayoutcode_gb300 import graphs as G
+            with tempfile.TemporaryDirectory() as td:
+                mtx, initf = os.path.join(td, "w.mtx"), os.path.join(td, "w.initf")
+                G.write_mtx(g, mtx)
+                G.write_initf(xy, initf)
+                it = max(1, min(steps, baseline_iters(w, g.n)))
+                out = subprocess.run([ref_bin, "-input", mtx, "-output", td + "/", "-iter", str(it), "-algo",
+                                      str(w["algo"]), "-batch", str(w["batch"]), "-bht", str(w["theta"]),
+                                      "-initf", initf, "-threads", str(cores)], cwd=td, capture_output=True,
+                                     text=True, timeout=1800)
+                m = re.search(r"Wall time required:([0-9.eE+-]+)", out.stdout)
+                if out.returncode == 0 and m:
+                    secs = float(m.group(1))
+                    value = g.n * it / secs
+                    kind = "reference"
+                    sample = f"{it} iterations of algo {w['algo']} (reference binary built from source, " \
+                             f"stock flags), reported wall time incl. file init"
+        except (OSError, subprocess.SubprocessError):
+            value = None
+    if value is None:
+        it = max(1, min(steps, baseline_iters(w, g.n))) * iters_per_step
+        value, secs = cpu_baseline_port(g, xy, w, it, cores)
+        sample = f"{it} iterations of algo {w['algo']} with the FP64 port (oracle/oracle.cpp, reference " \
+                 f"Makefile optimisation flags), same start, {cores} OpenMP threads"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{args.workload}: {w['desc']}"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="rgg1m", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    ws, rank, local = dist_env()
+    w = WORKLOADS[args.workload]
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        g, xy = load_workload(args.workload)
+        run_reference(args, w, g, xy)
+        return
+
+    import numpy as np
+    import torch
+
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    device = local if ws > 1 else 0
+
+    import batchlayoutcode_gb300 as B
+    B.build()
+    g, xy = load_workload(args.workload)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        it = baseline_iters(w, g.n)
+        v, secs = cpu_baseline_port(g, xy, w, it)
+        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"{it} iterations of algo {w['algo']} on the same graph from the same start, FP64 port "
+                         f"(oracle/oracle.cpp) with the reference Makefile's optimisation flags, "
+                         f"{os.cpu_count()} OpenMP threads, {secs:.1f} s"}
+
+    a = B.Algorithms(g.rowptr, g.colids, device=device)
+    a.nCoordinates = xy
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
+    algo, batch, theta = w["algo"], w["batch"], w["theta"]
+    decay = 0.999 if algo in (2, 4) else 0.99
+    step = 1.0
+    for _ in range(args.warmup):
+        a.run_resident(algo, 1, batch, theta, step)
+        step *= decay
+
+    kernel = KERNEL_FOR_ALGO[algo]
+    visits_before = None
+    if algo == 4:
+        _, (visits_before, _) = a.bh_repulsion(theta)
+    a.kernel_time(kernel)  # start timing the dominant kernel
+    launches0 = a.kernel_launches()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    times = []
+    with Clocks(device) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            a.run_resident(algo, 1, batch, theta, step)
+            times.append(a.last_run_ms())
+            step *= decay
+    torch.cuda.synchronize()
+    launches = a.kernel_launches() - launches0
+    kern_ms, kern_count = a.kernel_time()
+    total_ms = sum(times)
+    if dist:
+        t = torch.tensor([total_ms], device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = ws * g.n * args.steps / (total_ms / 1e3)
+    clocks = clk.summary()
+
+    # algorithmic bytes of the dominant kernel per launch
+    roof = None
+    pk = peaks()
+    if algo == 4:
+        _, (visits_after, _) = a.bh_repulsion(theta)
+        visits = 0.5 * (visits_before + visits_after)
+        alg_bytes = visits * 16.0
+        avg_s = kern_ms / max(kern_count, 1) / 1e3
+        achieved = alg_bytes / avg_s / 1e9
+        peak = pk["hbm_gbs"] if pk else 6800.0
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic_from_profile(kernel, args.workload),
+                "kernel": kernel, "kernel_ms_per_launch": avg_s * 1e3, "launches": kern_count,
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "fallback"}
+    else:
+        pairs = float(g.n) * g.n
+        avg_s = kern_ms / max(kern_count, 1) / 1e3
+        achieved = 10.0 * pairs / avg_s / 1e12
+        sm_mhz = (clocks or {}).get("sm_max_mhz") or (pk or {}).get("sm_max_mhz", 2070.0)
+        peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+        roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": traffic_from_profile(kernel, args.workload), "kernel": kernel,
+                "kernel_ms_per_launch": avg_s * 1e3, "launches": kern_count,
+                "algorithmic_flops_per_launch": 10.0 * pairs,
+                "peak_source": "nominal FP32 FMA peak: 152 SMs x 128 lanes x 2 flops x max SM clock"}
+
+    # end to end through the C ABI with pinned host buffers
+    host_in = torch.empty((g.n, 2), dtype=torch.float64, pin_memory=True)
+    host_out = torch.empty((g.n, 2), dtype=torch.float64, pin_memory=True)
+    host_in.copy_(torch.from_numpy(a.nCoordinates))
+    e2e_steps = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        a.set_coordinates_ptr(host_in.data_ptr())
+        if algo == 4:
+            a.barnes_hut_iteration(batch, theta, step)
+        else:
+            a.minibatch_iteration(algo, batch, step)
+        a.get_coordinates_ptr(host_out.data_ptr())
+        host_in.copy_(host_out)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": ws * g.n * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 16 * g.n,
+           "d2h_bytes_per_step": 16 * g.n + 8, "steps": e2e_steps}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{args.workload}: {w['desc']}", "vertices": g.n, "edges": g.nnz // 2,
+                       "step": "one layout iteration over the whole graph",
+                       "l2": "flushed before every timed step (256 MB write)",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    a.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

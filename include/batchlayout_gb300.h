@@ -1,0 +1,170 @@
+/*
+ * batchlayout_gb300.h -- C ABI of the GB300 BatchLayout layout engine.
+ *
+ * The reference (khaled-rahman/BatchLayoutCode) exposes its layout engine as
+ * the C++ class `algorithms` (sample/algorithms.h:50-85): a constructor that
+ * takes the CSR graph and the run options, one method per layout algorithm
+ * returning {energy, seconds} and mutating the coordinates, and writers for
+ * the `x<TAB>y<TAB>id` output file.  This header is the same interface as a
+ * plain C ABI: opaque context, plain pointers and sizes, int status codes.
+ *
+ * Conventions
+ *   - Coordinates cross the ABI as interleaved x,y pairs (2*n values), double
+ *     like the reference's Coordinate<double> (sample/Coordinate.h:27-85);
+ *     the device keeps them as float32.
+ *   - Every call returns BL_OK (0) or a negative BL_ERR_* code; the message is
+ *     available from bl_last_error().  Nothing exits or throws across the ABI.
+ *     (The reference prints and calls exit(1), e.g. sample/algorithms.cpp:104-106.)
+ *   - A context is used by one host thread at a time; it owns its CUDA stream
+ *     and device buffers.  No caller pointer is retained after a call returns.
+ *   - `threads` arguments are accepted for signature compatibility with the
+ *     reference (OpenMP thread count) and ignored.
+ */
+#ifndef BATCHLAYOUT_GB300_H
+#define BATCHLAYOUT_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BL_OK 0
+#define BL_ERR_ARG (-1)            /* invalid argument                      */
+#define BL_ERR_CUDA (-2)           /* CUDA runtime error                    */
+#define BL_ERR_DEVICE_TIMEOUT (-3) /* a device-side wait ran out of time    */
+#define BL_ERR_UNSUPPORTED (-4)    /* algorithm not on the GPU path         */
+#define BL_ERR_TOO_LARGE (-5)      /* problem exceeds a documented limit    */
+#define BL_ERR_IO (-6)             /* file could not be read or written     */
+#define BL_ERR_STATE (-7)          /* call order violated (e.g. no graph)   */
+
+typedef struct bl_ctx bl_ctx;
+
+/* ---- context -------------------------------------------------------------- */
+
+/* Replaces algorithms::algorithms(A_csr, input, outputd, init, weight, th, ifile)
+ * (sample/algorithms.cpp:3-15).  Copies the CSR (rowptr[n+1], colids[nnz],
+ * zero-based, as built by SetInputMatricesAsCSR, sample/commonutility.h:45-54)
+ * to the device.  init: 0 greedy DFS, 1 random, 2 file (`initfile`).
+ * Returns NULL on failure (bl_create_error() then holds the reason). */
+bl_ctx *bl_algorithms_create(int device, int n, long long nnz, const int *rowptr,
+                             const int *colids, const char *input,
+                             const char *outputdir, int init, double weight,
+                             double threshold, const char *initfile);
+const char *bl_create_error(void);
+void bl_destroy(bl_ctx *ctx);
+const char *bl_last_error(const bl_ctx *ctx);
+int bl_num_vertices(const bl_ctx *ctx);
+
+/* ---- input (host; the reference's L0 graph IO) ------------------------------ */
+
+/* SetInputMatricesAsCSR (sample/commonutility.h:45-54) = ReadASCII (IO.h:60-155)
+ * + CSC(triples) (CSC.h:147-190) + CSR(csc) (CSR.h:155-186): symmetric files are
+ * mirrored with self loops dropped, colids ascend within each row, duplicates
+ * are kept, values are ignored.  *rowptr / *colids are malloc'ed; release them
+ * with bl_free.  info[0..3] = rows, cols, nnz, symmetric; seconds = parse time.
+ * On error returns BL_ERR_IO and copies the reason into err (errcap bytes). */
+int bl_read_matrix_market(const char *path, long long *info, double *seconds, int **rowptr,
+                          int **colids, char *err, int errcap);
+void bl_free(void *p);
+
+/* ---- coordinates (the reference's nCoordinates) ---------------------------- */
+
+int bl_set_coordinates(bl_ctx *ctx, const double *xy, int n);
+int bl_get_coordinates(bl_ctx *ctx, double *xy, int n);
+/* Per-vertex forces of the last iteration run (the reference's prevCoordinates). */
+int bl_get_forces(bl_ctx *ctx, double *fxy, int n);
+
+/* ---- initialisers (host; sample/algorithms.cpp:16-119) --------------------- */
+
+/* randInit (:16-28) with a private glibc-compatible rand() stream seeded 1,
+ * i.e. the reference's sequence when it runs with one thread. */
+int bl_rand_init(bl_ctx *ctx);
+/* initDFS (:29-97): greedy DFS placement from vertex 0, same rand() stream. */
+int bl_init_dfs(bl_ctx *ctx);
+/* fileInitialization (:98-119): `x y id` lines read with "%lf %lf %d". */
+int bl_file_initialization(bl_ctx *ctx);
+
+/* Host-only forms of the same initialisers and of writeToFile: no context or
+ * GPU needed (xy holds 2*n doubles). */
+int bl_random_coordinates(int n, double *xy);
+int bl_greedy_coordinates(int n, const int *rowptr, const int *colids, double *xy);
+int bl_write_coordinates(const char *input, const char *outputdir, const char *tag,
+                         const double *xy, int n, char *path_out, int path_cap);
+
+/* ---- layout methods: out[0] = energy of the last iteration, out[1] = seconds
+ * (wall time including the init, like omp_get_wtime() in the reference).
+ * flag == 0 runs the context's initialiser first (init 0/1/2) and STEP = 1;
+ * flag == 1 keeps the current coordinates (and, for the minibatch methods,
+ * starts at STEP = 0.999^(4*iterations), sample/algorithms.cpp:737). ------ */
+
+/* algo 2: cacheBlockingminiBatchForceDirectedAlgorithm, sample/algorithms.cpp:715-794 */
+int bl_cache_blocking_minibatch(bl_ctx *ctx, int iterations, int threads, int batch,
+                                int flag, double *out);
+/* algo 2 with -engt: ...Converged, sample/algorithms.cpp:795-871; out[2] = loops run */
+int bl_cache_blocking_minibatch_converged(bl_ctx *ctx, int iterations, int threads,
+                                          int batch, int flag, double *out);
+/* algo 3: LinLogcacheBlockingminiBatchForceDirectedAlgorithm, :874-945 */
+int bl_linlog_cache_blocking_minibatch(bl_ctx *ctx, int iterations, int threads,
+                                       int batch, double *out);
+/* algo 8: FAcacheBlockingminiBatchForceDirectedAlgorithm, :947-1018 */
+int bl_fa_cache_blocking_minibatch(bl_ctx *ctx, int iterations, int threads, int batch,
+                                   double *out);
+/* algo 4: BarnesHutApproximation, :1020-1083 (theta = -bht) */
+int bl_barnes_hut_approximation(bl_ctx *ctx, int iterations, int threads, int batch,
+                                double theta, int flag, double *out);
+/* algo 6: approxCacheBlockBH, :1192-1215 (80% BH at theta 1.2, then algo 2) */
+int bl_approx_cache_block_bh(bl_ctx *ctx, int iterations, int threads, int batch,
+                             double *out);
+
+/* writeToFile (:1244-1256): outputdir + basename(input) + tag + ".txt",
+ * lines "x\ty\tid" at 6 significant digits.  The written path is copied to
+ * path_out (if not NULL, up to path_cap bytes). */
+int bl_write_to_file(bl_ctx *ctx, const char *tag, char *path_out, int path_cap);
+
+/* ---- building blocks exposed for verification and benchmarking ----------- */
+
+/* One minibatch iteration (the while-loop body of :742-780 / :895-933 /
+ * :968-1006) at the given STEP.  model: 2 FR, 3 LinLog, 8 FA.
+ * energy_out receives sum |f|^2 of this iteration. */
+int bl_minibatch_iteration(bl_ctx *ctx, int model, int batch, double step,
+                           double *energy_out);
+/* One Barnes-Hut iteration (the loop body of :1039-1071) at the given STEP. */
+int bl_barnes_hut_iteration(bl_ctx *ctx, int batch, double theta, double step,
+                            double *energy_out);
+
+/* Morton frame and order of the current coordinates (MortonCode.h:42-97,
+ * BarnesHut.h:121): frame = {minX, minY, MAXMIN}, keys[n] (y-major bit
+ * interleave of the two 32-bit quantised coordinates), perm[n]. */
+int bl_morton_order(bl_ctx *ctx, double *frame, unsigned long long *keys, int *perm);
+/* Quadtree of the current coordinates (BarnesHut.h:135-220) in canonical form:
+ * the nodes with at least two children, depth-first pre-order.  Returns the
+ * node count (>= 0) or a BL_ERR_* code; arrays must hold `cap` entries
+ * (centroid: 2*cap doubles). */
+int bl_quadtree(bl_ctx *ctx, int cap, int *lo, int *hi, int *depth, int *nchild,
+                double *centroid);
+/* Barnes-Hut repulsion sum (BarnesHut.h:69-86) for every vertex against the
+ * tree of the current coordinates; out[2n].  stats[0] = node visits,
+ * stats[1] = opening tests settled in FP64 (may be NULL). */
+int bl_bh_repulsion(bl_ctx *ctx, double theta, double *out, long long *stats);
+
+/* Device-resident run for throughput measurement: `iterations` iterations of
+ * algo (2, 3, 4 or 8) from the current device coordinates, no init, no host
+ * copies; STEP starts at `step` and decays as in the reference.
+ * energy_out = energy of the last iteration. */
+int bl_run_resident(bl_ctx *ctx, int algo, int iterations, int batch, double theta,
+                    double step, double *energy_out);
+/* Device time of the last bl_run_resident call: CUDA events recorded on the
+ * context's stream before its first and after its last kernel. */
+int bl_last_run_ms(bl_ctx *ctx, double *ms);
+/* Make the next bl_run_resident calls (same algo, batch, theta) replay a
+ * captured CUDA graph of one iteration (1) or launch kernels directly (0). */
+int bl_set_graph_mode(bl_ctx *ctx, int enabled);
+/* CUDA events around the dominant kernel of the last bl_run_resident call:
+ * ms[0] = total milliseconds of that kernel, ms[1] = number of launches. */
+int bl_last_kernel_time(bl_ctx *ctx, const char *kernel, double *ms);
+/* Number of kernels this library launched since the context was created. */
+long long bl_kernel_launches(const bl_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BATCHLAYOUT_GB300_H */

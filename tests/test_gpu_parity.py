@@ -1,0 +1,233 @@
+"""GPU parity: the CUDA path through the C ABI against the FP64 oracle and the
+reference's golden vectors.
+
+Tolerances (the layout computes forces in FP32 and keeps FP32 coordinates):
+  * force fields of one iteration: relative L2 <= 1e-5 against the FP64
+    oracle run from the same FP32 start on the same minibatch schedule;
+  * Morton keys, sort permutation, quadtree structure and FP64 centroids:
+    bit-exact;
+  * final energy after a full run: within 0.5% of the oracle's.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import GOLDEN_GRAPHS, load_golden
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-5
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def B():
+    import batchlayoutcode_gb300 as B
+    B.build()
+    return B
+
+
+@pytest.fixture(scope="module", params=GOLDEN_GRAPHS)
+def gold(request):
+    return request.param, load_golden(request.param)
+
+
+def make(B, z, **kw):
+    a = B.Algorithms(z["csr_rowptr"], z["csr_colids"], **kw)
+    a.nCoordinates = z["init_xy"]
+    return a
+
+
+@pytest.mark.parametrize("model", [2, 3, 8])
+@pytest.mark.parametrize("batch", [32, 256])
+def test_minibatch_iteration_forces(B, gold, model, batch):
+    _, z = gold
+    with make(B, z) as a:
+        e = a.minibatch_iteration(model, batch, 1.0)
+        f = a.prevCoordinates
+        xy = a.nCoordinates
+    oxy, of, oe = oracle.smu_iteration(model, z["csr_rowptr"], z["csr_colids"], z["init_xy"], batch, 1.0, 1.0)
+    assert rel_l2(f, of) <= FORCE_TOL
+    assert abs(e - oe) / oe <= 2 * FORCE_TOL
+    assert np.abs(xy - oxy).max() <= 1e-5
+
+
+@pytest.mark.parametrize("model", [2, 3, 8])
+def test_minibatch_jacobi_force_field(B, gold, model):
+    """batch = n: every force from the same start (pure force-field check)."""
+    _, z = gold
+    n = z["init_xy"].shape[0]
+    with make(B, z) as a:
+        a.minibatch_iteration(model, n, 1.0)
+        f = a.prevCoordinates
+    _, of, _ = oracle.smu_iteration(model, z["csr_rowptr"], z["csr_colids"], z["init_xy"], n, 1.0, 1.0)
+    assert rel_l2(f, of) <= FORCE_TOL
+
+
+@pytest.mark.parametrize("algo", [2, 3, 8])
+def test_minibatch_against_reference_golden(B, gold, algo):
+    _, z = gold
+    meth = {2: "cacheBlockingminiBatchForceDirectedAlgorithm",
+            3: "LinLogcacheBlockingminiBatchForceDirectedAlgorithm",
+            8: "FAcacheBlockingminiBatchForceDirectedAlgorithm"}[algo]
+    with B.Algorithms(z["csr_rowptr"], z["csr_colids"], init=2, ifile=_initf(gold[0])) as a:
+        e, _ = getattr(a, meth)(1, 1, 32) if algo != 2 else getattr(a, meth)(1, 1, 32, 0)
+        f = a.prevCoordinates
+    assert rel_l2(f, z[f"L{algo}_i1_f"]) <= FORCE_TOL
+    assert abs(e - float(z[f"L{algo}_i1_e"])) / float(z[f"L{algo}_i1_e"]) <= 2 * FORCE_TOL
+
+
+def _initf(name):
+    import os
+    from conftest import GOLDEN
+    return os.path.join(GOLDEN, f"{name}.initf")
+
+
+def test_morton_order_bit_exact(B, gold):
+    _, z = gold
+    with make(B, z) as a:
+        frame, keys, perm = a.morton_order()
+    xy32 = z["init_xy"].astype(np.float32).astype(np.float64)
+    oframe, okeys, operm = oracle.morton_sort(xy32)
+    assert np.array_equal(frame, oframe)
+    assert np.array_equal(keys, okeys)
+    assert np.array_equal(perm, operm)
+    # and the reference's own sort of the same points
+    assert np.array_equal(xy32[perm], z["bh_sorted"])
+
+
+def test_quadtree_bit_exact(B, gold):
+    _, z = gold
+    with make(B, z) as a:
+        t = a.quadtree()
+    for k in ("lo", "hi", "depth", "nchild"):
+        assert np.array_equal(t[k], z["tree_" + k]), k
+    assert np.array_equal(t["centroid"], z["tree_centroid"])
+
+
+@pytest.mark.parametrize("theta", [1.2, 0.5])
+def test_bh_repulsion(B, gold, theta):
+    _, z = gold
+    with make(B, z) as a:
+        rep, (visits, exact) = a.bh_repulsion(theta)
+    assert visits > 0
+    assert rel_l2(rep, z[f"bh_rep_t{theta}"]) <= FORCE_TOL
+
+
+@pytest.mark.parametrize("batch", [32, 256])
+def test_bh_iteration_forces(B, gold, batch):
+    _, z = gold
+    with make(B, z) as a:
+        e = a.barnes_hut_iteration(batch, 1.2, 1.0)
+        f = a.prevCoordinates
+        xy = a.nCoordinates
+    oxy, of, oe = oracle.bh_iteration(z["csr_rowptr"], z["csr_colids"], z["init_xy"], batch, 1.2, 1.0, 1.0)
+    assert rel_l2(f, of) <= FORCE_TOL
+    assert abs(e - oe) / oe <= 2 * FORCE_TOL
+    assert np.abs(xy - oxy).max() <= 1e-5
+
+
+def test_bh_against_reference_golden(B, gold):
+    name, z = gold
+    with B.Algorithms(z["csr_rowptr"], z["csr_colids"], init=2, ifile=_initf(name)) as a:
+        e, _ = a.BarnesHutApproximation(1, 1, 32, 1.2, 0)
+        f = a.prevCoordinates
+    assert rel_l2(f, z["L4_i1_f"]) <= FORCE_TOL
+    assert abs(e - float(z["L4_i1_e"])) / float(z["L4_i1_e"]) <= 2 * FORCE_TOL
+
+
+def test_run_is_deterministic(B, gold):
+    _, z = gold
+    outs = []
+    for _ in range(2):
+        with make(B, z) as a:
+            a.run_resident(2, 3, 32)
+            a.run_resident(4, 3, 32)
+            outs.append(a.nCoordinates)
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_converged_matches_oracle(B, gold):
+    name, z = gold
+    with B.Algorithms(z["csr_rowptr"], z["csr_colids"], init=2, ifile=_initf(name), th=0.05) as a:
+        e, _ = a.cacheBlockingminiBatchForceDirectedAlgorithmConverged(600, 1, 32, 0)
+        loops = a.loops
+    assert loops == int(z["conv_loops"])
+    assert abs(e - float(z["conv_e"])) / float(z["conv_e"]) <= 1e-3
+
+
+def test_algo6_energy(B, gold):
+    name, z = gold
+    with B.Algorithms(z["csr_rowptr"], z["csr_colids"], init=2, ifile=_initf(name)) as a:
+        e, _ = a.approxCacheBlockBH(4, 1, 32)
+    assert abs(e - float(z["L6_i4_e"])) / float(z["L6_i4_e"]) <= 1e-3
+
+
+@pytest.mark.parametrize("algo", [2, 4])
+def test_full_run_energy_within_half_percent(B, algo):
+    from batchlayoutcode_gb300 import graphs as G
+    g = G.grid_triangulated(24, 24)
+    xy = G.init_disc(g.n, 3)
+    with B.Algorithms(g.rowptr, g.colids) as a:
+        a.nCoordinates = xy
+        e = a.run_resident(algo, 300, 64, 1.2, 1.0)
+    _, oe, _ = oracle.layout(algo, g.rowptr, g.colids, xy.astype(np.float64), 300, 64)
+    assert abs(e - oe) / oe <= 5e-3
+
+
+def test_write_to_file_format(B, tmp_path):
+    name = "grid12"
+    z = load_golden(name)
+    with B.Algorithms(z["csr_rowptr"], z["csr_colids"], input="/x/y/grid12.mtx", outputd=str(tmp_path) + "/",
+                      init=2, ifile=_initf(name)) as a:
+        a.cacheBlockingminiBatchForceDirectedAlgorithm(3, 1, 32, 0)
+        path = a.writeToFile("CACHEMINB32PARAOUT3")
+    assert path == str(tmp_path) + "/grid12.mtxCACHEMINB32PARAOUT3.txt"
+    lines = open(path).read().splitlines()
+    ref = open(_golden_path("ref_output_grid12.txt")).read().splitlines()
+    assert len(lines) == len(ref)
+    got = np.array([[float(v) for v in l.split("\t")] for l in lines])
+    exp = np.array([[float(v) for v in l.split("\t")] for l in ref])
+    assert np.array_equal(got[:, 2], exp[:, 2])
+    assert np.abs(got[:, :2] - exp[:, :2]).max() < 1e-4
+
+
+def _golden_path(f):
+    import os
+    from conftest import GOLDEN
+    return os.path.join(GOLDEN, f)
+
+
+def test_cli_stdout_and_outputs_match_reference_layout(B, tmp_path):
+    import os
+    import subprocess
+    from conftest import GOLDEN, ROOT
+    exe = os.path.join(ROOT, "batchlayoutcode_gb300", "_build", "batchlayout")
+    mtx = os.path.join(GOLDEN, "grid12.mtx")
+    r = subprocess.run([exe, "-input", mtx, "-output", str(tmp_path) + "/", "-iter", "3", "-algo", "2",
+                        "-threads", "1", "-initf", os.path.join(GOLDEN, "grid12.initf"), "-batch", "32"],
+                       capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    got = r.stdout.splitlines()
+    ref = open(os.path.join(GOLDEN, "ref_stdout_grid12.txt")).read().splitlines()
+    assert len(got) == len(ref)
+    for k, (a, b) in enumerate(zip(got, ref)):
+        if ":" in b and k >= 10:
+            ka, va = a.split(":", 1)
+            kb, vb = b.split(":", 1)
+            assert ka == kb, (k, a, b)
+            if kb.endswith("Energy"):
+                assert abs(float(va) - float(vb)) / float(vb) < 1e-4
+        else:
+            assert a == b, (k, a, b)
+    # wrapper contract: line 18 wall time, line 19 output path (runBatchLayout.py:55-56)
+    assert got[18].startswith("Cache Blocking Minibatch Parallel Wall time required:")
+    out_path = got[19].split(":", 1)[1]
+    assert out_path == str(tmp_path) + "/grid12.mtxCACHEMINB32PARAOUT3.txt" and os.path.exists(out_path)
+    row = open(tmp_path / "Results.txt").read().strip().split("\t")
+    assert row[:5] == ["CACHE", "FILE", "3", "1", "32"]

@@ -1,0 +1,141 @@
+"""Host-side parts of the product (no GPU): C ABI surface, MatrixMarket reader,
+initialisers, writer, CLI argument handling, workload generators."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, GOLDEN_GRAPHS, ROOT, load_golden
+
+
+@pytest.fixture(scope="module")
+def L():
+    import batchlayoutcode_gb300 as B
+    B.build()
+    from batchlayoutcode_gb300 import _lib
+    return _lib
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "batchlayout_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(bl_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_header_symbol(L):
+    lib = L.load()
+    syms = header_symbols()
+    assert len(syms) >= 30
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    assert sorted(L.EXPORTS) == syms
+
+
+@pytest.mark.parametrize("name", GOLDEN_GRAPHS)
+def test_reader_matches_reference_csr(L, name):
+    z = load_golden(name)
+    rp, ci, info = L.read_matrix_market(os.path.join(GOLDEN, f"{name}.mtx"))
+    assert np.array_equal(rp, z["csr_rowptr"])
+    assert np.array_equal(ci, z["csr_colids"])
+    assert info["symmetric"] and info["nnz"] == len(z["csr_colids"])
+
+
+def test_reader_semantics(L, tmp_path):
+    # symmetric: mirrored, self loops dropped, duplicates kept, colids ascending
+    p = tmp_path / "s.mtx"
+    p.write_text("%%MatrixMarket matrix coordinate real symmetric\n% c\n4 4 5\n2 1 3.7\n3 3 1\n4 1 2\n4 2 1\n2 1 1\n")
+    rp, ci, info = L.read_matrix_market(str(p))
+    assert info["nnz"] == 8
+    assert rp.tolist() == [0, 3, 6, 6, 8]
+    assert ci.tolist() == [1, 1, 3, 0, 0, 3, 0, 1]
+    # general: taken as is (self loops kept)
+    p.write_text("%%MatrixMarket matrix coordinate pattern general\n3 3 3\n1 1\n3 1\n1 2\n")
+    rp, ci, info = L.read_matrix_market(str(p))
+    assert not info["symmetric"] and rp.tolist() == [0, 2, 2, 3] and ci.tolist() == [0, 1, 0]
+
+
+def test_reader_errors(L, tmp_path):
+    with pytest.raises(L.BatchLayoutError):
+        L.read_matrix_market(str(tmp_path / "missing.mtx"))
+    p = tmp_path / "bad.mtx"
+    p.write_text("%%MatrixMarket matrix coordinate pattern symmetric\n3 3 2\n1 7\n2 1\n")
+    with pytest.raises(L.BatchLayoutError):
+        L.read_matrix_market(str(p))
+    p.write_text("%%MatrixMarket matrix coordinate pattern symmetric\n3 3 4\n2 1\n")
+    with pytest.raises(L.BatchLayoutError):
+        L.read_matrix_market(str(p))
+
+
+@pytest.mark.parametrize("name", GOLDEN_GRAPHS)
+def test_greedy_init_bit_exact(L, name):
+    z = load_golden(name)
+    assert np.array_equal(L.greedy_coordinates(z["csr_rowptr"], z["csr_colids"]), z["init_greedy"])
+
+
+@pytest.mark.parametrize("name", GOLDEN_GRAPHS)
+def test_random_init_bit_exact(L, name):
+    z = load_golden(name)
+    assert np.array_equal(L.random_coordinates(len(z["csr_rowptr"]) - 1), z["init_rand1"])
+
+
+def test_writer_name_and_format(L, tmp_path):
+    xy = np.array([[1.2345678, -0.000123456789], [3e-7, 12345678.9]])
+    path = L.write_coordinates("/a/b/c.mtx", str(tmp_path) + "/", "CACHEMINB256PARAOUT600", xy)
+    assert path == str(tmp_path) + "/c.mtxCACHEMINB256PARAOUT600.txt"
+    lines = open(path).read().splitlines()
+    # default ostream formatting: 6 significant digits, like printf %g
+    assert lines == [f"{x:g}\t{y:g}\t{i + 1}" for i, (x, y) in enumerate(xy)]
+
+
+def test_writer_matches_reference_line_format():
+    ref = open(os.path.join(GOLDEN, "ref_output_grid12.txt")).read().splitlines()
+    for i, line in enumerate(ref):
+        x, y, idx = line.split("\t")
+        assert int(idx) == i + 1
+        assert f"{float(x):g}" == x and f"{float(y):g}" == y
+
+
+def cli():
+    import batchlayoutcode_gb300 as B
+    B.build()
+    return os.path.join(ROOT, "batchlayoutcode_gb300", "_build", "batchlayout")
+
+
+def test_cli_help_and_missing_input():
+    r = subprocess.run([cli(), "-h"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Usage of BatchLayout tool:" in r.stdout
+    assert "default: -weight 1.0 -bht 1.2 -engt 0.01 -batch 256 -iter 600 -threads MAX -algo 2 -init 0" in r.stdout
+    r = subprocess.run([cli()], capture_output=True, text=True)
+    assert r.returncode == 1 and "-input <string>" in r.stdout
+
+
+def test_cli_rejects_algorithms_off_the_gpu_path(tmp_path):
+    for algo in (0, 1, 5, 7):
+        r = subprocess.run([cli(), "-input", os.path.join(GOLDEN, "grid12.mtx"), "-algo", str(algo)],
+                           capture_output=True, text=True, cwd=tmp_path)
+        assert r.returncode == 3 and "not on the GPU layout path" in r.stderr
+        lines = r.stdout.splitlines()
+        ref = open(os.path.join(GOLDEN, "ref_stdout_grid12.txt")).read().splitlines()
+        assert lines[:10] == ref[:10]  # banner + reader lines as the reference prints them
+
+
+def test_product_does_not_use_the_oracle():
+    pkg = os.path.join(ROOT, "batchlayoutcode_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        if "_build" in dirpath:
+            continue
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".cpp", ".h")):
+                txt = open(os.path.join(dirpath, f)).read()
+                assert "import oracle" not in txt and "liboracle" not in txt, f
+
+
+def test_grid_generator_sizes():
+    from batchlayoutcode_gb300 import graphs as G
+    g = G.grid_triangulated(64, 64)
+    assert g.n == 4096 and g.nnz // 2 == 12033
+    assert np.all(np.diff(g.rowptr) > 0)
+    xy = G.init_disc(1000, 1)
+    assert xy.dtype == np.float32 and np.all((xy.astype(np.float64) ** 2).sum(1) <= 9.0 + 1e-6)
