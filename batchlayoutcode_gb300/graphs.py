@@ -161,10 +161,12 @@ def write_mtx(g: Graph, path: str) -> None:
 
 def write_initf(xy: np.ndarray, path: str) -> None:
     """`-initf` file: one `x y id` line per vertex (read with sscanf "%lf %lf %d",
-    sample/algorithms.cpp:112-116).  %.9g round-trips float32 exactly."""
-    xy = np.asarray(xy, dtype=np.float32)
+    sample/algorithms.cpp:112-116).  Each float32 value is written with the
+    shortest decimal that parses back (as a double) to exactly that value, so a
+    reader in FP64 and the float32 device layout start from the same numbers."""
+    xy = np.asarray(xy, dtype=np.float32).astype(np.float64)
     with open(path, "w") as f:
-        f.write("".join(f"{x:.9g} {y:.9g} {i + 1}\n" for i, (x, y) in enumerate(xy.tolist())))
+        f.write("".join(f"{x!r} {y!r} {i + 1}\n" for i, (x, y) in enumerate(xy.tolist())))
 
 
 def workload(name: str, seed: int = 1):

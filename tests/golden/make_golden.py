@@ -175,11 +175,11 @@ def main():
     # stdout layout of the stock CLI (line 18 = wall time, 19 = output path)
     with tempfile.TemporaryDirectory() as td:
         mtx = os.path.join(HERE, "grid12.mtx")
-        out = run([stock, "-input", mtx, "-output", td + "/", "-iter", "3", "-algo", "2", "-threads", "1",
+        out = run([stock, "-input", mtx, "-output", td + "/", "-iter", "1", "-algo", "2", "-threads", "1",
                    "-initf", os.path.join(HERE, "grid12.initf"), "-batch", str(BATCH)], cwd=td)
         with open(os.path.join(HERE, "ref_stdout_grid12.txt"), "w") as f:
             f.write(out.replace(td + "/", "<OUTDIR>/").replace(HERE + "/", "<GOLDEN>/"))
-        with open(os.path.join(td, "grid12.mtxCACHEMINB32PARAOUT3.txt")) as fin, \
+        with open(os.path.join(td, "grid12.mtxCACHEMINB32PARAOUT1.txt")) as fin, \
                 open(os.path.join(HERE, "ref_output_grid12.txt"), "w") as fout:
             fout.write(fin.read())
 
