@@ -102,7 +102,10 @@ void free_ctx(bl_ctx *c) {
   fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.visit); fr(s.qcen); fr(s.qbelow); fr(s.startcnt);
   fr(s.startbase); fr(s.scan_tmp); fr(s.nodes); fr(s.nodes_c64); fr(s.nodes_lvl); fr(s.rep);
   fr(s.stats); fr(s.pos_alt);
-  for (auto &ls : c->schedules) fr(ls.order);
+  for (auto &ls : c->schedules) {
+    fr(ls.order);
+    fr(ls.d_offsets);
+  }
   for (auto ev : c->ev_pool) cudaEventDestroy(ev);
   for (auto ev : c->run_ev)
     if (ev) cudaEventDestroy(ev);

@@ -99,127 +99,205 @@ __device__ __forceinline__ void frame_from_bbox(const unsigned int *bbox, double
   maxmin = (ry < rx) ? rx : ry;  // std::max(y-range, x-range)
 }
 
-// (uint32)(4294967295.0 * (v - mn) / maxmin), MortonCode.h:62-67, no contraction
-__device__ __forceinline__ unsigned int quantise(float v, double mn, double maxmin) {
+// (uint32)(4294967295.0 * (v - mn) / maxmin), MortonCode.h:62-67, no contraction.
+// The quotient is formed with the reciprocal (one multiply); its error is a
+// few ulp, so unless it lies within 4 ulp of an integer its truncation equals
+// the truncation of the correctly rounded quotient.  Otherwise the exact
+// division decides.
+__device__ __forceinline__ unsigned int quantise(float v, double mn, double maxmin, double inv) {
   if (!(maxmin > 0.0)) return 0u;
-  const double q = __ddiv_rn(__dmul_rn(4294967295.0, __dsub_rn((double)v, mn)), maxmin);
-  return __double2uint_rz(q);
+  const double a = __dmul_rn(4294967295.0, __dsub_rn((double)v, mn));
+  const double qf = __dmul_rn(a, inv);
+  const double fl = floor(qf);
+  const double eps = 4.0 * fabs(qf) * 1.1102230246251565e-16 + 1e-300;
+  if (qf - fl > eps && (fl + 1.0) - qf > eps) return __double2uint_rz(fl);
+  return __double2uint_rz(__ddiv_rn(a, maxmin));
 }
 
-__global__ void morton_kernel(const float2 *__restrict__ pos, int n, const unsigned int *bbox,
-                              u64 *keys, int *vals, double *frame) {
+__global__ void frame_kernel(const unsigned int *bbox, double *frame) {
+  if (threadIdx.x != 0) return;
   double minX, minY, maxmin;
   frame_from_bbox(bbox, minX, minY, maxmin);
+  frame[0] = minX;
+  frame[1] = minY;
+  frame[2] = maxmin;
+  frame[3] = (maxmin > 0.0) ? 1.0 / maxmin : 0.0;
+}
+
+__global__ void morton_kernel(const float2 *__restrict__ pos, int n, u64 *keys, int *vals,
+                              const double *__restrict__ frame) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) {
-    frame[0] = minX;
-    frame[1] = minY;
-    frame[2] = maxmin;
-  }
   if (i >= n) return;
+  const double minX = frame[0], minY = frame[1], maxmin = frame[2], inv = frame[3];
   const float2 p = pos[i];
-  keys[i] = (spread32(quantise(p.y, minY, maxmin)) << 1) | spread32(quantise(p.x, minX, maxmin));
+  keys[i] = (spread32(quantise(p.y, minY, maxmin, inv)) << 1) |
+            spread32(quantise(p.x, minX, maxmin, inv));
   vals[i] = i;
 }
 
-// ---- stable LSD radix sort, 8-bit digits ------------------------------------
+// ---- stable LSD radix sort, 8-bit digits, one kernel per digit pass -------
+//
+// Pass structure (decoupled look-back, after Adinets & Merrill, "Onesweep",
+// 2022): one kernel first counts all eight digit histograms; each pass then
+// takes tiles in launch order from an atomic counter, counts its tile's
+// digits, publishes those counts, ranks its keys stably, adds the counts of
+// the tiles before it (walking back until a tile that already published its
+// inclusive prefix) and scatters.  A tile that has published nothing yet is
+// waited for with a time bound; on timeout the pass records an error and the
+// waiting tile scatters nothing.
 constexpr int kRsThreads = 256;
 constexpr int kRsItems = 16;
 constexpr int kRsTile = kRsThreads * kRsItems;
+constexpr unsigned int kFlagAgg = 1u << 30, kFlagInc = 2u << 30, kCountMask = (1u << 30) - 1u;
+constexpr unsigned long long kLookbackTimeoutNs = 2000000000ull;
 
-__global__ void __launch_bounds__(kRsThreads) rs_hist_kernel(const u64 *__restrict__ keys, int n,
-                                                             int shift, unsigned int *hist,
-                                                             int nblocks) {
-  __shared__ unsigned int cnt[256];
-  cnt[threadIdx.x] = 0;
+// digit histograms of all 8 passes: hist8[pass * 256 + digit]
+__global__ void __launch_bounds__(1024) rs_hist8_kernel(const u64 *__restrict__ keys, int n,
+                                                        unsigned int *hist8) {
+  __shared__ unsigned int h[8 * 256];
+  for (int k = threadIdx.x; k < 8 * 256; k += blockDim.x) h[k] = 0;
   __syncthreads();
-  const int base = blockIdx.x * kRsTile;
-#pragma unroll 4
-  for (int r = 0; r < kRsItems; r++) {
-    const int idx = base + r * kRsThreads + threadIdx.x;
-    if (idx < n) atomicAdd(&cnt[(unsigned int)(keys[idx] >> shift) & 255u], 1u);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const u64 key = keys[i];
+#pragma unroll
+    for (int p = 0; p < 8; p++) atomicAdd(&h[p * 256 + (unsigned int)((key >> (8 * p)) & 255u)], 1u);
   }
   __syncthreads();
-  hist[threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
+  for (int k = threadIdx.x; k < 8 * 256; k += blockDim.x)
+    if (h[k]) atomicAdd(&hist8[k], h[k]);
 }
 
-// One block of 256 threads: thread d turns row d of hist into exclusive offsets
-// across blocks, then the digit totals are scanned and added.
-__global__ void __launch_bounds__(256) rs_scan_kernel(unsigned int *hist, int nblocks) {
-  __shared__ unsigned int tot[256];
-  const int d = threadIdx.x;
-  unsigned int run = 0;
-  unsigned int *row = hist + (size_t)d * nblocks;
-  int b = 0;
-  for (; b + 8 <= nblocks; b += 8) {
-    unsigned int v[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++) v[k] = row[b + k];
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-      row[b + k] = run;
-      run += v[k];
-    }
-  }
-  for (; b < nblocks; b++) {
-    const unsigned int v = row[b];
-    row[b] = run;
-    run += v;
-  }
-  tot[d] = run;
+// exclusive scan of each pass's 256 counts (block p scans pass p)
+__global__ void __launch_bounds__(256) rs_offsets_kernel(unsigned int *hist8) {
+  __shared__ unsigned int t[256];
+  unsigned int *row = hist8 + blockIdx.x * 256;
+  const unsigned int v = row[threadIdx.x];
+  t[threadIdx.x] = v;
   __syncthreads();
-  // exclusive scan of the 256 totals (Hillis-Steele on a copy)
-  unsigned int x = tot[d];
   for (int o = 1; o < 256; o <<= 1) {
+    const unsigned int y = (threadIdx.x >= (unsigned)o) ? t[threadIdx.x - o] : 0u;
     __syncthreads();
-    const unsigned int y = (d >= o) ? tot[d - o] : 0u;
+    t[threadIdx.x] += y;
     __syncthreads();
-    x += y;
-    tot[d] = x;
   }
-  __syncthreads();
-  const unsigned int excl = x - run;
-  for (b = 0; b < nblocks; b++) row[b] += excl;
+  row[threadIdx.x] = t[threadIdx.x] - v;
 }
 
-__global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
-    const u64 *__restrict__ kin, const int *__restrict__ vin, u64 *__restrict__ kout,
-    int *__restrict__ vout, int n, int shift, const unsigned int *__restrict__ offs, int nblocks) {
-  __shared__ unsigned int s_base[256];
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned int *p, unsigned int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+struct PassArgs {
+  const u64 *kin;
+  const int *vin;
+  u64 *kout;
+  int *vout;
+  int n, shift, ntiles;
+  const unsigned int *digit_off;  // 256 exclusive offsets of this pass
+  unsigned int *lookback;         // [ntiles][256] flag|count, zeroed before the pass
+  unsigned int *tile_counter;     // zeroed before the pass
+  DevStatus *st;
+};
+
+__global__ void __launch_bounds__(kRsThreads) rs_pass_kernel(PassArgs a) {
+  __shared__ unsigned int s_tile;
+  __shared__ unsigned int s_cnt[256];
+  __shared__ unsigned int s_run[256];
   __shared__ unsigned int s_w[kRsThreads / 32][256];
+  __shared__ unsigned int s_base[256];
+  __shared__ int s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  s_base[tid] = offs[(size_t)tid * nblocks + blockIdx.x];
-  const unsigned int lt = (1u << lane) - 1u;
-  const int base = blockIdx.x * kRsTile;
+  if (tid == 0) {
+    s_tile = atomicAdd(a.tile_counter, 1u);
+    s_abort = 0;
+  }
+  s_cnt[tid] = 0;
+  s_run[tid] = 0;
+  __syncthreads();
+  const int tile = (int)s_tile;
+  const int base = tile * kRsTile;
+  u64 key[kRsItems];
+  unsigned int dig[kRsItems];
+#pragma unroll
   for (int r = 0; r < kRsItems; r++) {
     const int idx = base + r * kRsThreads + tid;
-    const bool valid = idx < n;
-    const u64 key = valid ? kin[idx] : 0ull;
-    const unsigned int d = valid ? ((unsigned int)(key >> shift) & 255u) : 256u;
+    key[r] = (idx < a.n) ? a.kin[idx] : 0ull;
+    dig[r] = (idx < a.n) ? ((unsigned int)(key[r] >> a.shift) & 255u) : 256u;
+    if (dig[r] < 256u) atomicAdd(&s_cnt[dig[r]], 1u);
+  }
+  __syncthreads();
+  // publish this tile's counts as soon as they are known
+  unsigned int *my = a.lookback + (size_t)tile * 256;
+  if (tile == 0) st_release_u32(&my[tid], kFlagInc | s_cnt[tid]);
+  else st_release_u32(&my[tid], kFlagAgg | s_cnt[tid]);
+  // stable local ranks, one round of 256 keys at a time
+  unsigned int rank[kRsItems];
+  const unsigned int lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int r = 0; r < kRsItems; r++) {
 #pragma unroll
     for (int w = 0; w < kRsThreads / 32; w++) s_w[w][tid] = 0;
     __syncthreads();
-    const unsigned int peers = __match_any_sync(0xffffffffu, d);
-    const unsigned int rank = __popc(peers & lt);
-    if (valid && rank == 0) s_w[warp][d] = __popc(peers);
+    const unsigned int peers = __match_any_sync(0xffffffffu, dig[r]);
+    const unsigned int rk = __popc(peers & lt);
+    if (dig[r] < 256u && rk == 0) s_w[warp][dig[r]] = __popc(peers);
     __syncthreads();
     {
-      unsigned int run = s_base[tid];
+      unsigned int run = s_run[tid];
 #pragma unroll
       for (int w = 0; w < kRsThreads / 32; w++) {
         const unsigned int c = s_w[w][tid];
         s_w[w][tid] = run;
         run += c;
       }
-      s_base[tid] = run;
+      s_run[tid] = run;
     }
     __syncthreads();
-    if (valid) {
-      const unsigned int p = s_w[warp][d] + rank;
-      kout[p] = key;
-      vout[p] = vin[idx];
+    rank[r] = (dig[r] < 256u) ? s_w[warp][dig[r]] + rk : 0u;
+    __syncthreads();  // s_w is cleared at the top of the next round
+  }
+  // look back for the exclusive prefix of digit `tid` over earlier tiles
+  unsigned int excl = 0;
+  if (tile > 0) {
+    int t = tile - 1;
+    const unsigned long long t0 = dev_globaltimer();
+    while (t >= 0) {
+      const unsigned int v = ld_acquire_u32(&a.lookback[(size_t)t * 256 + tid]);
+      if (v & kFlagInc) {
+        excl += v & kCountMask;
+        break;
+      }
+      if (v & kFlagAgg) {
+        excl += v & kCountMask;
+        t--;
+        continue;
+      }
+      if (dev_globaltimer() - t0 > kLookbackTimeoutNs) {
+        dev_record_error(a.st, DEV_TIMEOUT_TREE);
+        s_abort = 1;
+        break;
+      }
     }
-    __syncthreads();
+    st_release_u32(&my[tid], kFlagInc | (excl + s_cnt[tid]));
+  }
+  s_base[tid] = a.digit_off[tid] + excl;
+  __syncthreads();
+  if (s_abort) return;
+#pragma unroll
+  for (int r = 0; r < kRsItems; r++) {
+    if (dig[r] < 256u) {
+      const int idx = base + r * kRsThreads + tid;
+      const unsigned int p = s_base[dig[r]] + rank[r];
+      if (p < (unsigned int)a.n) {
+        a.kout[p] = key[r];
+        a.vout[p] = a.vin[idx];
+      }
+    }
   }
 }
 
@@ -284,6 +362,24 @@ struct TreeArgs {
   int *startcnt;
 };
 
+// x / c for the child count c of a quad node, correctly rounded like the
+// reference's `c_x /= count` (BarnesHut.h:214-216) but without a division:
+// c = 2 and 4 scale exactly; for c = 3 the product with RN(1/3) is corrected
+// once with its exact FMA residual (Markstein, "IA-64 and Elementary
+// Functions", 2000), which is correctly rounded because x/3 is never a tie.
+__device__ __forceinline__ double div_count(double x, double c) {
+  if (c == 1.0) return x;
+  if (c == 2.0) return __dmul_rn(x, 0.5);
+  if (c == 4.0) return __dmul_rn(x, 0.25);
+  if (c == 3.0) {
+    const double r3 = 0.33333333333333331;  // RN(1/3)
+    const double q0 = __dmul_rn(x, r3);
+    const double r = __fma_rn(-3.0, q0, x);
+    return __fma_rn(r, r3, q0);
+  }
+  return __ddiv_rn(x, c);
+}
+
 // Internal node merged into its parent's quad node: the x-bit split of the
 // digit whose y-bit split is the parent, or any split inside a run of equal
 // keys below its top.
@@ -344,11 +440,20 @@ __device__ void process_quad(const TreeArgs &t, int node) {
     }
     if (kids[0] >= 0) below = __ldcg(&t.qbelow[kids[0]]) + 1;
   }
-  cx = __ddiv_rn(cx, cnt);
-  cy = __ddiv_rn(cy, cnt);
+  cx = div_count(cx, cnt);
+  cy = div_count(cy, cnt);
   t.qcen[node] = make_double2(cx, cy);
   t.qbelow[node] = below;
   if (node == 0) t.startcnt[rg.x] = below + 1;
+}
+
+// Arrival counter with acquire-release semantics at GPU scope: the release
+// publishes what this thread wrote for the subtree it finished, the acquire
+// makes the sibling thread's writes visible to the one that continues.
+__device__ __forceinline__ unsigned int arrive_acq_rel(unsigned int *p) {
+  unsigned int old;
+  asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  return old;
 }
 
 __global__ void bottomup_kernel(TreeArgs t) {
@@ -358,10 +463,8 @@ __global__ void bottomup_kernel(TreeArgs t) {
   // at most one step per tree level: the loop ends at the root (parent -1)
   // or at the first node this thread reaches before its sibling subtree
   while (node >= 0) {
-    __threadfence();
-    const unsigned int prev = atomicAdd(&t.visit[node], 1u);
+    const unsigned int prev = arrive_acq_rel(&t.visit[node]);
     if (prev == 0u) return;
-    __threadfence();
     if (!is_sub(t, node)) process_quad(t, node);
     node = (node == 0) ? -1 : t.parent[node];
   }
@@ -386,6 +489,7 @@ struct LayoutArgs {
 
 __global__ void layout_kernel(LayoutArgs L, TreeArgs t) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ld_volatile_u32(&L.st->code) != 0u) return;
   const double maxmin = L.frame[2];
   const int cap = 2 * L.n - 1;  // records: n leaves + at most n-1 quad nodes
   if (i < L.n) {  // leaf (sorted point) i
@@ -449,6 +553,7 @@ __device__ __noinline__ bool open_test_fp64(const double2 *__restrict__ c64,
 __global__ void __launch_bounds__(256) traverse_kernel(TraverseArgs a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= a.n) return;
+  if (ld_volatile_u32(&a.st->code) != 0u) return;  // the tree of this iteration is not valid
   const float2 q = a.spos[k];
   const float qm = fabsf(q.x) + fabsf(q.y);
   // record 0 is the root; its skip link is the number of records
@@ -500,8 +605,9 @@ __global__ void __launch_bounds__(256) traverse_kernel(TraverseArgs a) {
 }
 
 struct SweepArgs {
-  const int *order;
-  int lo, hi, batch;
+  const int *order;      // vertices grouped by dependency level
+  const int *level_off;  // levels + 1 offsets into order
+  int levels, batch;
   const int *rowptr;
   const int *colids;
   const float2 *pold;
@@ -509,40 +615,75 @@ struct SweepArgs {
   const float2 *rep;
   double2 *force;
   double *e;
+  int write_out;
   float W;
-  double step;
+  float step;
+  DevStatus *st;
 };
 
+constexpr int kSweepThreads = 1024;
+
 // Attraction over the CSR row in order (algorithms.cpp:1056-1058), minus the
-// BH repulsion (:1059), then the unit-step update (:1064).
-__global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a) {
-  const int t = a.lo + blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= a.hi) return;
-  const int i = a.order[t];
+// BH repulsion (:1059), then the unit-step update (:1064).  Forces are summed
+// in FP64 from FP32 terms; the unit vector and the step are FP32 (the new
+// coordinate is stored as float32 anyway).
+__device__ __forceinline__ void sweep_vertex(const SweepArgs &a, int i) {
   const float2 pi = a.pold[i];
-  const int bi = i / a.batch;
+  const int batch_lo = (i / a.batch) * a.batch;  // neighbours below it moved already
   double fx = 0.0, fy = 0.0;
   const int e1 = a.rowptr[i + 1];
-  for (int e = a.rowptr[i]; e < e1; e++) {
-    const int j = a.colids[e];
-    const float2 pj = (j / a.batch < bi) ? __ldcg(&a.pnew[j]) : a.pold[j];
-    const float dx = pj.x - pi.x, dy = pj.y - pi.y;
-    const float s = a.W * sqrtf(fmaf(dx, dx, dy * dy));
-    fx += (double)(dx * s);
-    fy += (double)(dy * s);
+  constexpr int kU = 4;  // issue the index loads, then the position loads, then sum in order
+  for (int e = a.rowptr[i]; e < e1; e += kU) {
+    int j[kU];
+    float2 pj[kU];
+#pragma unroll
+    for (int k = 0; k < kU; k++) j[k] = (e + k < e1) ? a.colids[e + k] : -1;
+#pragma unroll
+    for (int k = 0; k < kU; k++)
+      if (j[k] >= 0) pj[k] = (j[k] < batch_lo) ? __ldcg(&a.pnew[j[k]]) : a.pold[j[k]];
+#pragma unroll
+    for (int k = 0; k < kU; k++) {
+      if (j[k] < 0) break;
+      const float dx = pj[k].x - pi.x, dy = pj[k].y - pi.y;
+      const float sc = a.W * sqrtf(fmaf(dx, dx, dy * dy));
+      fx += (double)(dx * sc);
+      fy += (double)(dy * sc);
+    }
   }
   const float2 r = a.rep[i];
   fx -= (double)r.x;
   fy -= (double)r.y;
-  const double mag = sqrt(fx * fx + fy * fy);
   float2 np = pi;
-  if (mag > 0.0) {
-    np.x = (float)((double)pi.x + (fx / mag) * a.step);
-    np.y = (float)((double)pi.y + (fy / mag) * a.step);
+  const float fxf = (float)fx, fyf = (float)fy;
+  const float m2 = fmaf(fxf, fxf, fyf * fyf);
+  if (m2 >= 1.17549435e-38f && m2 <= 3.0e38f) {
+    const float rm = rsqrt_approx(m2);
+    np.x = fmaf(a.step, fxf * rm, pi.x);
+    np.y = fmaf(a.step, fyf * rm, pi.y);
+  } else if (fx != 0.0 || fy != 0.0) {  // outside the FP32 range of |f|^2
+    const double mag = sqrt(fx * fx + fy * fy);
+    np.x = (float)((double)pi.x + (fx / mag) * (double)a.step);
+    np.y = (float)((double)pi.y + (fy / mag) * (double)a.step);
   }
   a.pnew[i] = np;
-  a.force[i] = make_double2(fx, fy);
-  a.e[i] = fx * fx + fy * fy;
+  if (a.write_out) {
+    a.force[i] = make_double2(fx, fy);
+    a.e[i] = fx * fx + fy * fy;
+  }
+}
+
+// One cooperative launch for all dependency levels of an iteration; a
+// bounded grid barrier separates the levels.
+__global__ void __launch_bounds__(kSweepThreads) sweep_kernel(SweepArgs a) {
+  if (ld_volatile_u32(&a.st->code) != 0u) return;  // every block sees the same value: no barrier is left waiting
+  unsigned int epoch = 0;
+  const int gsz = gridDim.x * blockDim.x;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int l = 0; l < a.levels; l++) {
+    const int lo = a.level_off[l], hi = a.level_off[l + 1];
+    for (int t = lo + t0; t < hi; t += gsz) sweep_vertex(a, a.order[t]);
+    if (l + 1 < a.levels && !grid_barrier(a.st, epoch)) return;
+  }
 }
 
 inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
@@ -559,7 +700,7 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   fr(s.qbelow); fr(s.startcnt); fr(s.startbase); fr(s.nodes); fr(s.nodes_c64);
   fr(s.nodes_lvl); fr(s.rep); fr(s.pos_alt);
   const size_t nb = (n + kRsTile - 1) / kRsTile;
-  s.hist_entries = 256 * std::max<size_t>(nb, 1);
+  s.hist_entries = 8 * 256 + 8 + 8 * 256 * std::max<size_t>(nb, 1);
   const size_t m = std::max<size_t>(n, 2);
   BL_CUDA(ctx, cudaMalloc(&s.keys, m * 8));
   BL_CUDA(ctx, cudaMalloc(&s.keys_alt, m * 8));
@@ -595,19 +736,36 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   if (n < 2) return 0;
   bbox_init_kernel<<<1, 32, 0, st>>>(s.bbox);
   bbox_kernel<<<std::min(nblk(n, 256), ctx->num_sms * 4), 256, 0, st>>>(pos, n, s.bbox);
-  morton_kernel<<<nblk(n, 256), 256, 0, st>>>(pos, n, s.bbox, s.keys, s.perm, s.frame);
-  ctx->launches += 3;
+  frame_kernel<<<1, 32, 0, st>>>(s.bbox, s.frame);
+  morton_kernel<<<nblk(n, 256), 256, 0, st>>>(pos, n, s.keys, s.perm, s.frame);
+  ctx->launches += 4;
   const int nb = nblk(n, kRsTile);
   unsigned long long *kin = s.keys, *kout = s.keys_alt;
   int *vin = s.perm, *vout = s.perm_alt;
+  // hist layout: [8 passes x 256 digit offsets][8 tile counters][8 x ntiles x 256 look-back]
+  unsigned int *hist8 = s.hist, *counters = s.hist + 8 * 256, *lookback = s.hist + 8 * 256 + 8;
   bl_time_begin(ctx, "radix_sort");
-  for (int shift = 0; shift < 64; shift += 8) {
-    rs_hist_kernel<<<nb, kRsThreads, 0, st>>>(kin, n, shift, s.hist, nb);
-    rs_scan_kernel<<<1, 256, 0, st>>>(s.hist, nb);
-    rs_scatter_kernel<<<nb, kRsThreads, 0, st>>>(kin, vin, kout, vout, n, shift, s.hist, nb);
+  BL_CUDA(ctx, cudaMemsetAsync(s.hist, 0, (8 * 256 + 8 + (size_t)8 * nb * 256) * sizeof(unsigned int), st));
+  rs_hist8_kernel<<<ctx->num_sms, 1024, 0, st>>>(kin, n, hist8);
+  rs_offsets_kernel<<<8, 256, 0, st>>>(hist8);
+  ctx->launches += 2;
+  for (int pass = 0; pass < 8; pass++) {
+    PassArgs pa;
+    pa.kin = kin;
+    pa.vin = vin;
+    pa.kout = kout;
+    pa.vout = vout;
+    pa.n = n;
+    pa.shift = 8 * pass;
+    pa.ntiles = nb;
+    pa.digit_off = hist8 + pass * 256;
+    pa.lookback = lookback + (size_t)pass * nb * 256;
+    pa.tile_counter = counters + pass;
+    pa.st = s.status;
+    rs_pass_kernel<<<nb, kRsThreads, 0, st>>>(pa);
     std::swap(kin, kout);
     std::swap(vin, vout);
-    ctx->launches += 3;
+    ctx->launches++;
   }
   bl_time_end(ctx, "radix_sort");
   // 8 passes: sorted data is back in keys/perm
@@ -690,6 +848,8 @@ int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_en
   if (int rc = bh_traverse(ctx, theta, false)) return rc;
   SweepArgs a;
   a.order = ls->order;
+  a.level_off = ls->d_offsets;
+  a.levels = ls->levels;
   a.batch = batch;
   a.rowptr = ctx->g.rowptr;
   a.colids = ctx->g.colids;
@@ -698,18 +858,24 @@ int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_en
   a.rep = ctx->s.rep;
   a.force = ctx->force;
   a.e = ctx->e;
+  a.write_out = want_energy ? 1 : 0;
   a.W = (float)ctx->weight;
-  a.step = step;
-  bl_time_begin(ctx, "sweep_kernel");
-  for (int l = 0; l < ls->levels; l++) {
-    a.lo = ls->offsets[l];
-    a.hi = ls->offsets[l + 1];
-    if (a.hi <= a.lo) continue;
-    sweep_kernel<<<nblk(a.hi - a.lo, 256), 256, 0, ctx->stream>>>(a);
-    ctx->launches++;
+  a.step = (float)step;
+  a.st = ctx->s.status;
+  static int sweep_grid = 0;
+  if (sweep_grid == 0) {
+    int occ = 0;
+    BL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sweep_kernel, kSweepThreads, 0));
+    if (occ < 1) return bl_fail(ctx, -5, "sweep kernel cannot be resident");
+    sweep_grid = ctx->num_sms;
   }
+  BL_CUDA(ctx, cudaMemsetAsync(&ctx->s.status->barrier, 0, sizeof(unsigned int), ctx->stream));
+  void *args[] = {&a};
+  bl_time_begin(ctx, "sweep_kernel");
+  BL_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)sweep_kernel, dim3(sweep_grid), dim3(kSweepThreads),
+                                           args, 0, ctx->stream));
   bl_time_end(ctx, "sweep_kernel");
-  BL_CUDA(ctx, cudaGetLastError());
+  ctx->launches++;
   std::swap(ctx->pos, ctx->s.pos_alt);
   if (want_energy) {
     if (int rc = energy_reduce(ctx, energy_out)) return rc;
@@ -806,8 +972,14 @@ const LevelSchedule *level_schedule(bl_ctx *ctx, int batch) {
   std::vector<int> order(std::max(n, 1));
   std::vector<int> fill(ls.offsets.begin(), ls.offsets.end() - 1);
   for (int i = 0; i < n; i++) order[fill[lev[i]]++] = i;
-  if (cudaMalloc(&ls.order, order.size() * sizeof(int)) != cudaSuccess) {
+  if (cudaMalloc(&ls.order, order.size() * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&ls.d_offsets, ls.offsets.size() * sizeof(int)) != cudaSuccess) {
     bl_fail(ctx, -2, "cudaMalloc level schedule");
+    return nullptr;
+  }
+  if (cudaMemcpy(ls.d_offsets, ls.offsets.data(), ls.offsets.size() * sizeof(int), cudaMemcpyHostToDevice) !=
+      cudaSuccess) {
+    bl_fail(ctx, -2, "cudaMemcpy level schedule");
     return nullptr;
   }
   if (cudaMemcpy(ls.order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {

@@ -126,6 +126,7 @@ struct LevelSchedule {
   int levels = 0;
   std::vector<int> offsets;  // host copy, levels + 1 entries
   int *order = nullptr;      // device: vertices grouped by level
+  int *d_offsets = nullptr;  // device copy of offsets
 };
 
 struct Scratch {

@@ -70,6 +70,9 @@ def lib(fast: bool = False) -> C.CDLL:
     L.orc_bh_iteration.argtypes = [C.c_int, _i32p, _i32p, _f64p, C.c_int, C.c_double, C.c_double,
                                    C.c_double, C.c_void_p, C.c_int]
     L.orc_bh_iteration.restype = C.c_double
+    L.orc_forces_on_trajectory.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, C.c_int, C.c_double,
+                                           C.c_double, _f64p, C.c_int]
+    L.orc_forces_on_trajectory.restype = C.c_double
     _libs[fast] = L
     return L
 
@@ -148,3 +151,17 @@ def bh_iteration(rowptr, colids, xy, batch: int, theta: float, weight: float, st
                                np.ascontiguousarray(colids, np.int32), pos.ravel(), batch, theta, weight,
                                step, forces.ctypes.data, _threads(nthreads))
     return pos, forces, e
+
+
+def forces_on_trajectory(algo: int, rowptr, colids, xy_start, xy_end, batch: int, theta: float = 1.2,
+                         weight: float = 1.0, nthreads=None):
+    """Forces of one iteration where batch b is evaluated from the state
+    {xy_end for earlier batches, xy_start otherwise}: the reference's step
+    re-seeded from another implementation's batch-start states.  -> (forces, energy)"""
+    a = np.ascontiguousarray(xy_start, dtype=np.float64)
+    b = np.ascontiguousarray(xy_end, dtype=np.float64)
+    f = np.zeros_like(a)
+    e = lib().orc_forces_on_trajectory(algo, a.shape[0], np.ascontiguousarray(rowptr, np.int32),
+                                       np.ascontiguousarray(colids, np.int32), a.ravel(), b.ravel(), batch, theta,
+                                       weight, f.ravel(), _threads(nthreads))
+    return f, e

@@ -79,9 +79,12 @@ inline void apply_update(P2 &p, double fx, double fy, double step) {
 // The j loop is blocked by 512 with a fresh accumulator per block (:753-771),
 // and the sorted-CSR cursor kindex (:746,758-762) decides whether a source is
 // a neighbour (attraction) or not (repulsion).
+// `replay` (optional): instead of moving a batch by its own forces, set it to
+// replay[i] -- the positions another implementation produced -- so that every
+// batch is evaluated from that implementation's batch-start state.
 double smu_iteration(int model, int n, const int *rowptr, const int *colids,
                      P2 *pos, int batch, double W, double step, P2 *force_out,
-                     int nthreads) {
+                     int nthreads, const P2 *replay = nullptr) {
   const int blocky = 512;
   const long long nnz = rowptr[n];
   std::vector<P2> prev(n, P2{0.0, 0.0});
@@ -121,7 +124,8 @@ double smu_iteration(int model, int n, const int *rowptr, const int *colids,
       prev[i] = P2{px, py};
     }
     for (int i = i0; i < i1; i++) {
-      apply_update(pos[i], prev[i].x, prev[i].y, step);
+      if (replay) pos[i] = replay[i];
+      else apply_update(pos[i], prev[i].x, prev[i].y, step);
       energy += prev[i].x * prev[i].x + prev[i].y * prev[i].y;
     }
   }
@@ -330,7 +334,7 @@ void bh_force(const Tree &t, int node, const P2 &v, double theta, double &fx,
 // One pass of the BarnesHutApproximation loop body (sample/algorithms.cpp:1039-1071).
 double bh_iteration(int n, const int *rowptr, const int *colids, P2 *pos,
                     int batch, double theta, double W, double step,
-                    P2 *force_out, int nthreads) {
+                    P2 *force_out, int nthreads, const P2 *replay = nullptr) {
   std::vector<P2> prev(n, P2{0.0, 0.0});
   Tree t;
   Frame fr;
@@ -356,7 +360,8 @@ double bh_iteration(int n, const int *rowptr, const int *colids, P2 *pos,
       prev[i] = P2{fx - rx, fy - ry};
     }
     for (int i = i0; i < i1; i++) {
-      apply_update(pos[i], prev[i].x, prev[i].y, step);
+      if (replay) pos[i] = replay[i];
+      else apply_update(pos[i], prev[i].x, prev[i].y, step);
       energy += prev[i].x * prev[i].x + prev[i].y * prev[i].y;
     }
   }
@@ -548,6 +553,23 @@ double orc_bh_iteration(int n, const int *rowptr, const int *colids, double *xy,
   return bh_iteration(n, rowptr, colids, reinterpret_cast<P2 *>(xy), batch,
                       theta, W, step, reinterpret_cast<P2 *>(force_out),
                       nthreads);
+}
+
+// Forces of one iteration evaluated on another implementation's trajectory:
+// batch b sees xy_end for the batches before it and xy_start for the rest
+// (its batch-start state in that implementation).  algo 2/3/8 (minibatch
+// models) or 4 (Barnes-Hut, tree and queries from xy_start).  Returns the
+// energy; force_out receives 2n values.
+double orc_forces_on_trajectory(int algo, int n, const int *rowptr, const int *colids,
+                                const double *xy_start, const double *xy_end, int batch,
+                                double theta, double W, double *force_out, int nthreads) {
+  std::vector<P2> pos(reinterpret_cast<const P2 *>(xy_start),
+                      reinterpret_cast<const P2 *>(xy_start) + n);
+  const P2 *rep = reinterpret_cast<const P2 *>(xy_end);
+  P2 *fo = reinterpret_cast<P2 *>(force_out);
+  if (algo == 4)
+    return bh_iteration(n, rowptr, colids, pos.data(), batch, theta, W, 1.0, fo, nthreads, rep);
+  return smu_iteration(algo, n, rowptr, colids, pos.data(), batch, W, 1.0, fo, nthreads, rep);
 }
 
 }  // extern "C"
