@@ -99,12 +99,14 @@ void free_ctx(bl_ctx *c) {
   bl::Scratch &s = c->s;
   fr(s.energy_parts); fr(s.energy); fr(s.status); fr(s.partials); fr(s.keys); fr(s.keys_alt);
   fr(s.perm); fr(s.perm_alt); fr(s.hist); fr(s.bbox); fr(s.frame); fr(s.spos); fr(s.bparent);
-  fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.visit); fr(s.qcen); fr(s.qbelow); fr(s.startcnt);
+  fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.qkids); fr(s.lvl_list); fr(s.lvl); fr(s.qcen); fr(s.qbelow); fr(s.startcnt);
   fr(s.startbase); fr(s.scan_tmp); fr(s.nodes); fr(s.nodes_c64); fr(s.nodes_lvl); fr(s.rep);
-  fr(s.stats); fr(s.pos_alt);
+  fr(s.stats); fr(s.pos_alt); fr(s.f0);
   for (auto &ls : c->schedules) {
     fr(ls.order);
     fr(ls.d_offsets);
+    fr(ls.early_off);
+    fr(ls.early_col);
   }
   for (auto ev : c->ev_pool) cudaEventDestroy(ev);
   for (auto ev : c->run_ev)
@@ -529,7 +531,7 @@ int bl_bh_repulsion(bl_ctx *ctx, double theta, double *out, long long *stats) {
   const int n = ctx->g.n;
   if (int rc = bl::ensure_bh_scratch(ctx)) return rc;
   if (int rc = bl::bh_build(ctx, ctx->pos)) return rc;
-  if (int rc = bl::bh_traverse(ctx, theta, true)) return rc;
+  if (int rc = bl::bh_traverse(ctx, theta, true, 0)) return rc;
   std::vector<float2> rep(n);
   unsigned long long st[2] = {0, 0};
   BL_CUDA(ctx, cudaMemcpyAsync(rep.data(), ctx->s.rep, (size_t)n * sizeof(float2), cudaMemcpyDeviceToHost, ctx->stream));

@@ -29,6 +29,7 @@
 //      and batch size) and each level is one parallel launch.  This produces
 //      the same values as the reference's sequential batch loop.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 
@@ -350,34 +351,39 @@ __global__ void radix_tree_kernel(const u64 *__restrict__ K, int n, int2 *child,
 
 struct TreeArgs {
   int n;
-  const u64 *keys;
   const float2 *spos;
   const int2 *child;
   const int2 *range;
   const int *dlt;
   const int *parent;
-  unsigned int *visit;
+  int4 *qkids;          // quad children of a quad node, kNoChild-padded
   double2 *qcen;
   int *qbelow;
   int *startcnt;
+  unsigned int *lvl;    // [33 counts][33 cursors][34 segment offsets]
+  int *lvl_list;        // quad nodes, deepest digit level first
+  DevStatus *st;
 };
+
+constexpr int kNoChild = INT_MIN;
+constexpr int kLevels = 33;  // digit levels 0..31 plus 32 for runs of equal keys
 
 // x / c for the child count c of a quad node, correctly rounded like the
 // reference's `c_x /= count` (BarnesHut.h:214-216) but without a division:
 // c = 2 and 4 scale exactly; for c = 3 the product with RN(1/3) is corrected
 // once with its exact FMA residual (Markstein, "IA-64 and Elementary
 // Functions", 2000), which is correctly rounded because x/3 is never a tie.
-__device__ __forceinline__ double div_count(double x, double c) {
-  if (c == 1.0) return x;
-  if (c == 2.0) return __dmul_rn(x, 0.5);
-  if (c == 4.0) return __dmul_rn(x, 0.25);
-  if (c == 3.0) {
+__device__ __forceinline__ double div_count(double x, int c) {
+  if (c == 1) return x;
+  if (c == 2) return __dmul_rn(x, 0.5);
+  if (c == 4) return __dmul_rn(x, 0.25);
+  if (c == 3) {
     const double r3 = 0.33333333333333331;  // RN(1/3)
     const double q0 = __dmul_rn(x, r3);
     const double r = __fma_rn(-3.0, q0, x);
     return __fma_rn(r, r3, q0);
   }
-  return __ddiv_rn(x, c);
+  return __ddiv_rn(x, (double)c);
 }
 
 // Internal node merged into its parent's quad node: the x-bit split of the
@@ -391,82 +397,138 @@ __device__ __forceinline__ bool is_sub(const TreeArgs &t, int node) {
   return (p & 1) && (pp == p - 1);
 }
 
-__device__ void process_quad(const TreeArgs &t, int node) {
-  const int p = t.dlt[node];
-  const int2 rg = t.range[node];
-  double cx = 0.0, cy = 0.0, cnt = 0.0;
-  int below = 0;
-  if (p >= 64) {
-    // run of identical keys: every point is a child (the reference recurses
-    // without end here; see the oracle's note)
-    for (int k = rg.x; k <= rg.y; k++) {
-      const float2 q = t.spos[k];
-      cx = __dadd_rn(cx, (double)q.x);
-      cy = __dadd_rn(cy, (double)q.y);
-      cnt += 1.0;
-    }
-  } else {
-    int kids[4];
-    int m = 0;
-    const int2 ab = t.child[node];
-    const int sides[2] = {ab.x, ab.y};
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const int c = sides[h];
-      if (c >= 0 && is_sub(t, c)) {
-        const int2 cc = t.child[c];
-        kids[m++] = cc.x;
-        kids[m++] = cc.y;
-      } else {
-        kids[m++] = c;
-      }
-    }
-    for (int q = 0; q < m; q++) {
-      const int c = kids[q];
-      double vx, vy;
-      if (c < 0) {
-        const float2 pt = t.spos[~c];
-        vx = (double)pt.x;
-        vy = (double)pt.y;
-      } else {
-        const double2 v = __ldcg(&t.qcen[c]);
-        vx = v.x;
-        vy = v.y;
-        if (q > 0) t.startcnt[__ldcg(&t.range[c].x)] = __ldcg(&t.qbelow[c]) + 1;
-      }
-      cx = __dadd_rn(cx, vx);
-      cy = __dadd_rn(cy, vy);
-      cnt += 1.0;
-    }
-    if (kids[0] >= 0) below = __ldcg(&t.qbelow[kids[0]]) + 1;
-  }
-  cx = div_count(cx, cnt);
-  cy = div_count(cy, cnt);
-  t.qcen[node] = make_double2(cx, cy);
-  t.qbelow[node] = below;
-  if (node == 0) t.startcnt[rg.x] = below + 1;
-}
+__device__ __forceinline__ int quad_level(int p) { return p >= 64 ? 32 : (p >> 1); }
 
-// Arrival counter with acquire-release semantics at GPU scope: the release
-// publishes what this thread wrote for the subtree it finished, the acquire
-// makes the sibling thread's writes visible to the one that continues.
-__device__ __forceinline__ unsigned int arrive_acq_rel(unsigned int *p) {
-  unsigned int old;
-  asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
-  return old;
-}
-
-__global__ void bottomup_kernel(TreeArgs t) {
+// Structure of the quadtree, one thread per sorted position k.  The binary
+// nodes whose range starts at k form the left-child chain above leaf k; the
+// chains of different k are disjoint, so each thread owns its nodes and no
+// synchronisation is needed.  For every quad node on the chain it records the
+// number of quad nodes below it on the chain (qbelow) and its quad children;
+// startcnt[k] counts the quad nodes starting at k.  Digit-level counts are
+// gathered per block for the level-ordered centroid pass.
+__global__ void __launch_bounds__(256) chain_kernel(TreeArgs t) {
+  __shared__ unsigned int hist[kLevels];
+  if (threadIdx.x < kLevels) hist[threadIdx.x] = 0;
+  __syncthreads();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= t.n) return;
-  int node = t.parent[t.n - 1 + k];
-  // at most one step per tree level: the loop ends at the root (parent -1)
-  // or at the first node this thread reaches before its sibling subtree
-  while (node >= 0) {
-    const unsigned int prev = arrive_acq_rel(&t.visit[node]);
-    if (prev == 0u) return;
-    if (!is_sub(t, node)) process_quad(t, node);
-    node = (node == 0) ? -1 : t.parent[node];
+  if (k < t.n) {
+    int cnt = 0;
+    int cur = t.parent[t.n - 1 + k];
+    // bounded by the tree height: every step moves to a parent
+    while (cur >= 0 && t.range[cur].x == k) {
+      if (!is_sub(t, cur)) {
+        t.qbelow[cur] = cnt++;
+        int kids[4] = {kNoChild, kNoChild, kNoChild, kNoChild};
+        const int p = t.dlt[cur];
+        if (p < 64) {
+          int m = 0;
+          const int2 ab = t.child[cur];
+          const int sides[2] = {ab.x, ab.y};
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            const int c = sides[h];
+            if (c >= 0 && is_sub(t, c)) {
+              const int2 cc = t.child[c];
+              kids[m++] = cc.x;
+              kids[m++] = cc.y;
+            } else {
+              kids[m++] = c;
+            }
+          }
+        }
+        t.qkids[cur] = make_int4(kids[0], kids[1], kids[2], kids[3]);
+        atomicAdd(&hist[quad_level(p)], 1u);
+      }
+      cur = (cur == 0) ? -1 : t.parent[cur];
+    }
+    t.startcnt[k] = cnt;
+  }
+  __syncthreads();
+  if (threadIdx.x < kLevels && hist[threadIdx.x]) atomicAdd(&t.lvl[threadIdx.x], hist[threadIdx.x]);
+}
+
+// segment offsets, deepest level first: seg s holds digit level 32 - s
+__global__ void level_offsets_kernel(unsigned int *lvl) {
+  if (threadIdx.x != 0) return;
+  unsigned int run = 0;
+  for (int s = 0; s < kLevels; s++) {
+    lvl[2 * kLevels + s] = run;
+    run += lvl[32 - s];
+  }
+  lvl[2 * kLevels + kLevels] = run;
+}
+
+__global__ void __launch_bounds__(256) level_fill_kernel(TreeArgs t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool quad = (i < t.n - 1) && !is_sub(t, i);
+  const int seg = quad ? 32 - quad_level(t.dlt[i]) : -1;
+  const unsigned int active = __ballot_sync(0xffffffffu, quad);
+  if (!quad) return;
+  const unsigned int peers = __match_any_sync(active, seg);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  unsigned int base = 0;
+  if (lane == leader) base = atomicAdd(&t.lvl[kLevels + seg], (unsigned int)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  const unsigned int rank = __popc(peers & ((1u << lane) - 1u));
+  t.lvl_list[t.lvl[2 * kLevels + seg] + base + rank] = i;
+}
+
+// Centroids, deepest digit level first, with a bounded grid barrier between
+// levels: the unweighted mean of the children summed in quadrant order in
+// FP64 (BarnesHut.h:197-217), bit-identical to the reference.
+__global__ void __launch_bounds__(1024) centroid_kernel(TreeArgs t) {
+  if (ld_volatile_u32(&t.st->code) != 0u) return;
+  unsigned int epoch = 0;
+  const int gsz = gridDim.x * blockDim.x;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned int *seg_off = t.lvl + 2 * kLevels;
+  int last = -1;
+  for (int sg = 0; sg < kLevels; sg++)
+    if (seg_off[sg + 1] > seg_off[sg]) last = sg;
+  for (int sg = 0; sg <= last; sg++) {
+    const int lo = (int)seg_off[sg], hi = (int)seg_off[sg + 1];
+    if (hi == lo) continue;
+    for (int q = lo + t0; q < hi; q += gsz) {
+      const int node = t.lvl_list[q];
+      const int p = t.dlt[node];
+      double cx = 0.0, cy = 0.0;
+      int cnt = 0;
+      if (p >= 64) {
+        // run of identical keys: every point is a child (the reference
+        // recurses without end here; see the oracle's note)
+        const int2 rg = t.range[node];
+        for (int k = rg.x; k <= rg.y; k++) {
+          const float2 v = t.spos[k];
+          cx = __dadd_rn(cx, (double)v.x);
+          cy = __dadd_rn(cy, (double)v.y);
+          cnt++;
+        }
+      } else {
+        const int4 kk = t.qkids[node];
+        const int kids[4] = {kk.x, kk.y, kk.z, kk.w};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const int ch = kids[c];
+          if (ch == kNoChild) break;
+          double vx, vy;
+          if (ch < 0) {
+            const float2 v = t.spos[~ch];
+            vx = (double)v.x;
+            vy = (double)v.y;
+          } else {
+            const double2 v = __ldcg(&t.qcen[ch]);
+            vx = v.x;
+            vy = v.y;
+          }
+          cx = __dadd_rn(cx, vx);
+          cy = __dadd_rn(cy, vy);
+          cnt++;
+        }
+      }
+      t.qcen[node] = make_double2(div_count(cx, cnt), div_count(cy, cnt));
+    }
+    if (sg < last && !grid_barrier(t.st, epoch)) return;
   }
 }
 
@@ -536,7 +598,25 @@ struct TraverseArgs {
   float theta2;
   double theta;
   unsigned long long *stats;  // [visits, fp64 decisions] or null
+  // attraction of neighbours that have not moved yet in this iteration
+  // (same or later batch), summed with the repulsion into f0; null to skip
+  float4 *f0;
+  const int *rowptr;
+  const int *colids;
+  const float2 *pold;
+  int batch;
+  float W;
 };
+
+// Compensated float-float accumulation (Knuth's TwoSum): hi + lo carries the
+// sum of FP32 terms to about 48 bits without touching the FP64 pipe.
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float t) {
+  const float s = hi + t;
+  const float bb = s - hi;
+  const float err = (hi - (s - bb)) + (t - bb);
+  hi = s;
+  lo += err;
+}
 
 // FP64 opening test exactly as BarnesHut.h:71-72: diameter / distance < theta.
 __device__ __noinline__ bool open_test_fp64(const double2 *__restrict__ c64,
@@ -597,7 +677,26 @@ __global__ void __launch_bounds__(256) traverse_kernel(TraverseArgs a) {
       i++;
     }
   }
-  a.rep[a.perm[k]] = make_float2(fx, fy);
+  const int v = a.perm[k];
+  a.rep[v] = make_float2(fx, fy);
+  if (a.f0) {
+    // FR attraction (algorithms.cpp:1056-1058) over the neighbours j that are
+    // not moved before v in this iteration (j at or after v's batch start)
+    const float2 pv = a.pold[v];
+    const int batch_lo = (v / a.batch) * a.batch;
+    float hx = -fx, lx = 0.f, hy = -fy, ly = 0.f;
+    const int e1 = a.rowptr[v + 1];
+    for (int e = a.rowptr[v]; e < e1; e++) {
+      const int j = a.colids[e];
+      if (j < batch_lo) continue;
+      const float2 pj = a.pold[j];
+      const float dx = pj.x - pv.x, dy = pj.y - pv.y;
+      const float sc = a.W * sqrtf(fmaf(dx, dx, dy * dy));
+      ff_add(hx, lx, dx * sc);
+      ff_add(hy, ly, dy * sc);
+    }
+    a.f0[v] = make_float4(hx, hy, lx, ly);
+  }
   if (a.stats) {
     atomicAdd(&a.stats[0], (unsigned long long)visits);
     if (exact) atomicAdd(&a.stats[1], (unsigned long long)exact);
@@ -607,12 +706,12 @@ __global__ void __launch_bounds__(256) traverse_kernel(TraverseArgs a) {
 struct SweepArgs {
   const int *order;      // vertices grouped by dependency level
   const int *level_off;  // levels + 1 offsets into order
-  int levels, batch;
-  const int *rowptr;
-  const int *colids;
+  const int *early_off;  // per level-order slot: earlier-batch neighbours
+  const int *early_col;
+  int levels;
+  const float4 *f0;      // attraction of unmoved neighbours minus repulsion (float-float)
   const float2 *pold;
   float2 *pnew;
-  const float2 *rep;
   double2 *force;
   double *e;
   int write_out;
@@ -623,50 +722,38 @@ struct SweepArgs {
 
 constexpr int kSweepThreads = 1024;
 
-// Attraction over the CSR row in order (algorithms.cpp:1056-1058), minus the
-// BH repulsion (:1059), then the unit-step update (:1064).  Forces are summed
-// in FP64 from FP32 terms; the unit vector and the step are FP32 (the new
-// coordinate is stored as float32 anyway).
-__device__ __forceinline__ void sweep_vertex(const SweepArgs &a, int i) {
+// Adds the attraction of the neighbours that moved earlier in this iteration
+// (earlier batches, their new positions) to f0, then the unit-step update
+// (algorithms.cpp:1056-1066).  FP32 terms, float-float sum, FP32 unit vector.
+__device__ __forceinline__ void sweep_vertex(const SweepArgs &a, int t) {
+  const int i = a.order[t];
   const float2 pi = a.pold[i];
-  const int batch_lo = (i / a.batch) * a.batch;  // neighbours below it moved already
-  double fx = 0.0, fy = 0.0;
-  const int e1 = a.rowptr[i + 1];
-  constexpr int kU = 4;  // issue the index loads, then the position loads, then sum in order
-  for (int e = a.rowptr[i]; e < e1; e += kU) {
-    int j[kU];
-    float2 pj[kU];
-#pragma unroll
-    for (int k = 0; k < kU; k++) j[k] = (e + k < e1) ? a.colids[e + k] : -1;
-#pragma unroll
-    for (int k = 0; k < kU; k++)
-      if (j[k] >= 0) pj[k] = (j[k] < batch_lo) ? __ldcg(&a.pnew[j[k]]) : a.pold[j[k]];
-#pragma unroll
-    for (int k = 0; k < kU; k++) {
-      if (j[k] < 0) break;
-      const float dx = pj[k].x - pi.x, dy = pj[k].y - pi.y;
-      const float sc = a.W * sqrtf(fmaf(dx, dx, dy * dy));
-      fx += (double)(dx * sc);
-      fy += (double)(dy * sc);
-    }
+  const float4 f = a.f0[i];
+  float hx = f.x, hy = f.y, lx = f.z, ly = f.w;
+  const int e1 = a.early_off[t + 1];
+  for (int e = a.early_off[t]; e < e1; e++) {
+    const float2 pj = __ldcg(&a.pnew[a.early_col[e]]);
+    const float dx = pj.x - pi.x, dy = pj.y - pi.y;
+    const float sc = a.W * sqrtf(fmaf(dx, dx, dy * dy));
+    ff_add(hx, lx, dx * sc);
+    ff_add(hy, ly, dy * sc);
   }
-  const float2 r = a.rep[i];
-  fx -= (double)r.x;
-  fy -= (double)r.y;
+  const float fxf = hx + lx, fyf = hy + ly;
   float2 np = pi;
-  const float fxf = (float)fx, fyf = (float)fy;
   const float m2 = fmaf(fxf, fxf, fyf * fyf);
   if (m2 >= 1.17549435e-38f && m2 <= 3.0e38f) {
     const float rm = rsqrt_approx(m2);
     np.x = fmaf(a.step, fxf * rm, pi.x);
     np.y = fmaf(a.step, fyf * rm, pi.y);
-  } else if (fx != 0.0 || fy != 0.0) {  // outside the FP32 range of |f|^2
+  } else if (fxf != 0.f || fyf != 0.f) {  // |f|^2 outside the FP32 range
+    const double fx = (double)hx + (double)lx, fy = (double)hy + (double)ly;
     const double mag = sqrt(fx * fx + fy * fy);
     np.x = (float)((double)pi.x + (fx / mag) * (double)a.step);
     np.y = (float)((double)pi.y + (fy / mag) * (double)a.step);
   }
   a.pnew[i] = np;
   if (a.write_out) {
+    const double fx = (double)hx + (double)lx, fy = (double)hy + (double)ly;
     a.force[i] = make_double2(fx, fy);
     a.e[i] = fx * fx + fy * fy;
   }
@@ -674,14 +761,14 @@ __device__ __forceinline__ void sweep_vertex(const SweepArgs &a, int i) {
 
 // One cooperative launch for all dependency levels of an iteration; a
 // bounded grid barrier separates the levels.
-__global__ void __launch_bounds__(kSweepThreads) sweep_kernel(SweepArgs a) {
+__global__ void __launch_bounds__(kSweepThreads, 2) sweep_kernel(SweepArgs a) {
   if (ld_volatile_u32(&a.st->code) != 0u) return;  // every block sees the same value: no barrier is left waiting
   unsigned int epoch = 0;
   const int gsz = gridDim.x * blockDim.x;
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
   for (int l = 0; l < a.levels; l++) {
     const int lo = a.level_off[l], hi = a.level_off[l + 1];
-    for (int t = lo + t0; t < hi; t += gsz) sweep_vertex(a, a.order[t]);
+    for (int t = lo + t0; t < hi; t += gsz) sweep_vertex(a, t);
     if (l + 1 < a.levels && !grid_barrier(a.st, epoch)) return;
   }
 }
@@ -696,9 +783,10 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   if (s.bh_n >= n && s.keys) return 0;
   auto fr = [](void *p) { if (p) cudaFree(p); };
   fr(s.keys); fr(s.keys_alt); fr(s.perm); fr(s.perm_alt); fr(s.hist); fr(s.spos);
-  fr(s.bparent); fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.visit); fr(s.qcen);
+  fr(s.bparent); fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.qkids); fr(s.lvl_list); fr(s.lvl);
+  fr(s.qcen);
   fr(s.qbelow); fr(s.startcnt); fr(s.startbase); fr(s.nodes); fr(s.nodes_c64);
-  fr(s.nodes_lvl); fr(s.rep); fr(s.pos_alt);
+  fr(s.nodes_lvl); fr(s.rep); fr(s.f0); fr(s.pos_alt);
   const size_t nb = (n + kRsTile - 1) / kRsTile;
   s.hist_entries = 8 * 256 + 8 + 8 * 256 * std::max<size_t>(nb, 1);
   const size_t m = std::max<size_t>(n, 2);
@@ -712,7 +800,9 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   BL_CUDA(ctx, cudaMalloc(&s.bchild, m * sizeof(int2)));
   BL_CUDA(ctx, cudaMalloc(&s.brange, m * sizeof(int2)));
   BL_CUDA(ctx, cudaMalloc(&s.bdelta, m * sizeof(int)));
-  BL_CUDA(ctx, cudaMalloc(&s.visit, m * sizeof(unsigned int)));
+  BL_CUDA(ctx, cudaMalloc(&s.qkids, m * sizeof(int4)));
+  BL_CUDA(ctx, cudaMalloc(&s.lvl_list, m * sizeof(int)));
+  BL_CUDA(ctx, cudaMalloc(&s.lvl, 3 * 34 * sizeof(unsigned int)));
   BL_CUDA(ctx, cudaMalloc(&s.qcen, m * sizeof(double2)));
   BL_CUDA(ctx, cudaMalloc(&s.qbelow, m * sizeof(int)));
   BL_CUDA(ctx, cudaMalloc(&s.startcnt, (m + 1) * sizeof(int)));
@@ -721,6 +811,7 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   BL_CUDA(ctx, cudaMalloc(&s.nodes_c64, 2 * m * sizeof(double2)));
   BL_CUDA(ctx, cudaMalloc(&s.nodes_lvl, 2 * m));
   BL_CUDA(ctx, cudaMalloc(&s.rep, m * sizeof(float2)));
+  BL_CUDA(ctx, cudaMalloc(&s.f0, m * sizeof(float4)));
   BL_CUDA(ctx, cudaMalloc(&s.pos_alt, m * sizeof(float2)));
   s.bh_n = n;
   return 0;
@@ -771,22 +862,32 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   // 8 passes: sorted data is back in keys/perm
   gather_kernel<<<nblk(n, 256), 256, 0, st>>>(pos, s.perm, n, s.spos);
   radix_tree_kernel<<<nblk(n - 1, 256), 256, 0, st>>>(s.keys, n, s.bchild, s.brange, s.bdelta, s.bparent);
-  BL_CUDA(ctx, cudaMemsetAsync(s.visit, 0, (size_t)n * sizeof(unsigned int), st));
-  BL_CUDA(ctx, cudaMemsetAsync(s.startcnt, 0, (size_t)(n + 1) * sizeof(int), st));
+  BL_CUDA(ctx, cudaMemsetAsync(s.lvl, 0, 3 * 34 * sizeof(unsigned int), st));
+  BL_CUDA(ctx, cudaMemsetAsync(s.startcnt + n, 0, sizeof(int), st));
   TreeArgs t;
   t.n = n;
-  t.keys = s.keys;
   t.spos = s.spos;
   t.child = s.bchild;
   t.range = s.brange;
   t.dlt = s.bdelta;
   t.parent = s.bparent;
-  t.visit = s.visit;
+  t.qkids = s.qkids;
   t.qcen = s.qcen;
   t.qbelow = s.qbelow;
   t.startcnt = s.startcnt;
-  bottomup_kernel<<<nblk(n, 256), 256, 0, st>>>(t);
-  ctx->launches += 3;
+  t.lvl = s.lvl;
+  t.lvl_list = s.lvl_list;
+  t.st = s.status;
+  chain_kernel<<<nblk(n, 256), 256, 0, st>>>(t);
+  level_offsets_kernel<<<1, 32, 0, st>>>(s.lvl);
+  level_fill_kernel<<<nblk(n - 1, 256), 256, 0, st>>>(t);
+  BL_CUDA(ctx, cudaMemsetAsync(&s.status->barrier, 0, sizeof(unsigned int), st));
+  {
+    void *args[] = {&t};
+    BL_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)centroid_kernel, dim3(ctx->num_sms), dim3(1024), args,
+                                             0, st));
+  }
+  ctx->launches += 6;
   if (int rc = scan_exclusive_int(ctx, s.startcnt, s.startbase, n + 1)) return rc;
   LayoutArgs L;
   L.n = n;
@@ -809,7 +910,7 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   return 0;
 }
 
-int bh_traverse(bl_ctx *ctx, double theta, bool want_stats) {
+int bh_traverse(bl_ctx *ctx, double theta, bool want_stats, int batch) {
   const int n = ctx->g.n;
   Scratch &s = ctx->s;
   if (n < 2) {
@@ -829,6 +930,12 @@ int bh_traverse(bl_ctx *ctx, double theta, bool want_stats) {
   a.theta2 = (float)(theta * theta);
   a.stats = want_stats ? s.stats : nullptr;
   a.st = s.status;
+  a.f0 = batch > 0 ? s.f0 : nullptr;
+  a.rowptr = ctx->g.rowptr;
+  a.colids = ctx->g.colids;
+  a.pold = ctx->pos;
+  a.batch = batch > 0 ? batch : 1;
+  a.W = (float)ctx->weight;
   if (want_stats) BL_CUDA(ctx, cudaMemsetAsync(s.stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
   bl_time_begin(ctx, "traverse_kernel");
   traverse_kernel<<<nblk(n, 256), 256, 0, ctx->stream>>>(a);
@@ -845,30 +952,26 @@ int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_en
   if (!ls) return -2;
   float2 *pold = ctx->pos, *pnew = ctx->s.pos_alt;
   if (int rc = bh_build(ctx, pold)) return rc;
-  if (int rc = bh_traverse(ctx, theta, false)) return rc;
+  if (int rc = bh_traverse(ctx, theta, false, batch)) return rc;
   SweepArgs a;
   a.order = ls->order;
   a.level_off = ls->d_offsets;
+  a.early_off = ls->early_off;
+  a.early_col = ls->early_col;
   a.levels = ls->levels;
-  a.batch = batch;
-  a.rowptr = ctx->g.rowptr;
-  a.colids = ctx->g.colids;
+  a.f0 = ctx->s.f0;
   a.pold = pold;
   a.pnew = pnew;
-  a.rep = ctx->s.rep;
   a.force = ctx->force;
   a.e = ctx->e;
   a.write_out = want_energy ? 1 : 0;
   a.W = (float)ctx->weight;
   a.step = (float)step;
   a.st = ctx->s.status;
-  static int sweep_grid = 0;
-  if (sweep_grid == 0) {
-    int occ = 0;
-    BL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sweep_kernel, kSweepThreads, 0));
-    if (occ < 1) return bl_fail(ctx, -5, "sweep kernel cannot be resident");
-    sweep_grid = ctx->num_sms;
-  }
+  int occ = 0;
+  BL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sweep_kernel, kSweepThreads, 0));
+  if (occ < 1) return bl_fail(ctx, -5, "sweep kernel cannot be resident");
+  const int sweep_grid = ctx->num_sms * std::min(occ, 2);
   BL_CUDA(ctx, cudaMemsetAsync(&ctx->s.status->barrier, 0, sizeof(unsigned int), ctx->stream));
   void *args[] = {&a};
   bl_time_begin(ctx, "sweep_kernel");
@@ -984,6 +1087,24 @@ const LevelSchedule *level_schedule(bl_ctx *ctx, int batch) {
   }
   if (cudaMemcpy(ls.order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
     bl_fail(ctx, -2, "cudaMemcpy level schedule");
+    return nullptr;
+  }
+  // neighbours in earlier batches, per level-order slot, in CSR order
+  std::vector<int> eoff(std::max(n, 1) + 1, 0), ecol;
+  ecol.reserve(ci.size() / 2 + 1);
+  for (int t = 0; t < n; t++) {
+    const int i = order[t];
+    const int blo = (i / batch) * batch;
+    for (int e = rp[i]; e < rp[i + 1]; e++)
+      if (ci[e] < blo) ecol.push_back(ci[e]);
+    eoff[t + 1] = (int)ecol.size();
+  }
+  if (ecol.empty()) ecol.push_back(0);
+  if (cudaMalloc(&ls.early_off, eoff.size() * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&ls.early_col, ecol.size() * sizeof(int)) != cudaSuccess ||
+      cudaMemcpy(ls.early_off, eoff.data(), eoff.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ls.early_col, ecol.data(), ecol.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+    bl_fail(ctx, -2, "level schedule neighbour lists");
     return nullptr;
   }
   ctx->schedules.push_back(std::move(ls));

@@ -127,6 +127,8 @@ struct LevelSchedule {
   std::vector<int> offsets;  // host copy, levels + 1 entries
   int *order = nullptr;      // device: vertices grouped by level
   int *d_offsets = nullptr;  // device copy of offsets
+  int *early_off = nullptr;  // per level-order slot: neighbours in earlier batches
+  int *early_col = nullptr;
 };
 
 struct Scratch {
@@ -150,7 +152,9 @@ struct Scratch {
   int2 *bchild = nullptr;        // children of internal node (encoded: >= 0 internal, < 0 leaf ~k)
   int2 *brange = nullptr;        // [first, last] of internal node
   int *bdelta = nullptr;         // common prefix length of internal node
-  unsigned int *visit = nullptr; // bottom-up arrival counters
+  int4 *qkids = nullptr;         // quad children of a quad node
+  int *lvl_list = nullptr;       // quad nodes ordered by digit level, deepest first
+  unsigned int *lvl = nullptr;   // level counts, cursors, segment offsets
   double2 *qcen = nullptr;       // centroid of quad node (indexed by binary internal id)
   int *qbelow = nullptr;         // chain length below a quad node
   int *startcnt = nullptr;       // quad nodes starting at each sorted position (n+1)
@@ -160,6 +164,7 @@ struct Scratch {
   double2 *nodes_c64 = nullptr;  // FP64 centroid per pre-order record
   unsigned char *nodes_lvl = nullptr;
   float2 *rep = nullptr;         // BH repulsion per vertex
+  float4 *f0 = nullptr;          // unmoved-neighbour attraction minus repulsion (float-float)
   unsigned long long *stats = nullptr;
   float2 *pos_alt = nullptr;     // second position buffer (Gauss-Seidel sweep)
 };
@@ -218,7 +223,7 @@ int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step
                   double *energy_out, long long *loops_out);
 int ensure_bh_scratch(bl_ctx *ctx);
 int bh_build(bl_ctx *ctx, const float2 *pos);
-int bh_traverse(bl_ctx *ctx, double theta, bool want_stats);
+int bh_traverse(bl_ctx *ctx, double theta, bool want_stats, int batch);
 int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_energy,
                  double *energy_out);
 int bh_canonical_tree(bl_ctx *ctx, int cap, int *lo, int *hi, int *depth, int *nchild,
