@@ -23,6 +23,7 @@ EXPORTS = (
     "bl_write_to_file", "bl_minibatch_iteration", "bl_barnes_hut_iteration", "bl_morton_order",
     "bl_quadtree", "bl_bh_repulsion", "bl_run_resident", "bl_set_graph_mode", "bl_last_kernel_time",
     "bl_kernel_launches", "bl_last_run_ms", "bl_random_coordinates", "bl_greedy_coordinates", "bl_write_coordinates",
+    "bl_minibatch_iteration_noalloc",
 )
 
 _lib = None
@@ -79,6 +80,7 @@ def load() -> C.CDLL:
         "bl_random_coordinates": (i32, [i32, dp]),
         "bl_greedy_coordinates": (i32, [i32, ip, ip, dp]),
         "bl_write_coordinates": (i32, [cp, cp, cp, dp, i32, cp, i32]),
+        "bl_minibatch_iteration_noalloc": (i32, [i32, vp, vp, vp, vp, vp, i32, i32, f64, f64, dp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

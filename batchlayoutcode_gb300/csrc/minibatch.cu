@@ -28,7 +28,9 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <mutex>
 
+#include "../../include/batchlayout_gb300.h"
 #include "bl_internal.cuh"
 
 namespace bl {
@@ -364,3 +366,134 @@ int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step
 }
 
 }  // namespace bl
+
+// ---------------------------------------------------------------------------
+// Allocation-free entry point.
+//
+// Some callers cannot allocate device memory once they are running: services
+// that reserve all GPU memory up front in their own pool, real-time loops
+// that forbid allocation after start-up, or code that enqueues work on a
+// stream another component owns.  bl_minibatch_iteration_noalloc runs the
+// same minibatch kernel as bl_minibatch_iteration, but every scratch buffer
+// it needs (partial forces, energy partials, the device status word) lives
+// in the fixed array below, so the call allocates nothing.  The caller passes
+// its inputs and outputs as device pointers.
+//
+// Limits: batch <= 256 and at most 160 blocks (one per SM), so the scratch is
+// at most 2 * 256 * 160 float2 partials plus a few hundred bytes: 768 KiB.
+// The array exists once per device for the lifetime of the process and every
+// call on that device shares it: calls that overlap on the GPU (different
+// streams, or host threads that do not serialise) race and give wrong
+// results.  The first call on a device looks up the array's device address
+// (cudaGetSymbolAddress) with that device current; make that first call
+// before any stream capture.
+// ---------------------------------------------------------------------------
+namespace bl {
+namespace {
+
+constexpr int kNoAllocMaxBatch = 256;
+constexpr int kNoAllocMaxGrid = 160;
+constexpr size_t kNoAllocPartialBytes = (size_t)2 * kNoAllocMaxBatch * kNoAllocMaxGrid * sizeof(float2);
+constexpr size_t kNoAllocBytes = 768 * 1024;
+static_assert(kNoAllocPartialBytes + kNoAllocMaxGrid * sizeof(double) + 4 * sizeof(double) +
+                      sizeof(DevStatus) <= kNoAllocBytes,
+              "no-alloc scratch too small");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+unsigned char *g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+}  // namespace
+}  // namespace bl
+
+extern "C" int bl_minibatch_iteration_noalloc(int n, const int *d_rowptr, const int *d_colids,
+                                              float *d_xy, double *d_force, double *d_vertex_energy,
+                                              int model, int batch, double weight, double step,
+                                              double *energy_out, void *stream) {
+  using namespace bl;
+  if (n < 1 || !d_rowptr || !d_colids || !d_xy || !d_force || !d_vertex_energy)
+    return BL_ERR_ARG;
+  if (model != MODEL_FR && model != MODEL_LINLOG && model != MODEL_FA) return BL_ERR_ARG;
+  if (batch < 1) return BL_ERR_ARG;
+  batch = std::min(batch, n);
+  if (batch > kNoAllocMaxBatch) return BL_ERR_TOO_LARGE;  // scratch holds batch <= 256
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) return BL_ERR_CUDA;
+  unsigned char *base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+      void *p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return BL_ERR_CUDA;
+      g_noalloc_ptr[device] = static_cast<unsigned char *>(p);
+    }
+    base = g_noalloc_ptr[device];
+  }
+  int num_sms = 0, smem_optin = 0;
+  cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device);
+  cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  // same block count and shared-memory sizing as the context path
+  int grid = std::min(num_sms, std::max(1, (n + 127) / 128));
+  auto smem_for = [&](int g) {
+    const int slice_max = (n + g - 1) / g + 2;
+    return (size_t)(((slice_max + 3) & ~3) + (kGroups - 1) * kChunk + batch) * sizeof(float2);
+  };
+  while (smem_for(grid) + 1024 > (size_t)smem_optin && grid < num_sms) grid++;
+  if (grid > kNoAllocMaxGrid) return BL_ERR_TOO_LARGE;  // scratch holds 160 blocks of partials
+  const size_t smem = smem_for(grid);
+  if (smem + 1024 > (size_t)smem_optin) return BL_ERR_TOO_LARGE;
+  if (cudaFuncSetAttribute(minibatch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return BL_ERR_CUDA;
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, minibatch_kernel, kThreads, smem) != cudaSuccess ||
+      occ < 1 || grid > occ * num_sms)
+    return BL_ERR_TOO_LARGE;
+  // carve the scratch: partials | energy parts | energy + loops | status
+  float2 *partials = reinterpret_cast<float2 *>(base);
+  double *energy_parts = reinterpret_cast<double *>(base + kNoAllocPartialBytes);
+  double *energy = energy_parts + kNoAllocMaxGrid;
+  DevStatus *status = reinterpret_cast<DevStatus *>(energy + 4);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // the status word (barrier counter, error code) must start at zero; every
+  // other scratch value is written before it is read
+  if (cudaMemsetAsync(status, 0, sizeof(DevStatus), st) != cudaSuccess) return BL_ERR_CUDA;
+  MinibatchArgs a;
+  a.n = n;
+  a.batch = batch;
+  a.nbatches = (n + batch - 1) / batch;
+  a.model = model;
+  a.grid = grid;
+  a.W = weight;
+  a.eff_rowptr = d_rowptr;
+  a.eff_colids = d_colids;
+  a.pos = reinterpret_cast<float2 *>(d_xy);
+  a.force = reinterpret_cast<double2 *>(d_force);
+  a.e = d_vertex_energy;
+  a.partials = partials;
+  a.energy = energy;
+  a.energy_parts = energy_parts;
+  a.loops = reinterpret_cast<long long *>(energy + 1);
+  a.st = status;
+  a.iterations = 1;
+  a.step0 = step;
+  a.decay = 1.0;
+  a.converged = 0;
+  a.engt = 0.0;
+  a.max_loops = 0;
+  void *args[] = {&a};
+  if (cudaLaunchCooperativeKernel((const void *)minibatch_kernel, dim3(grid), dim3(kThreads), args, smem, st) !=
+      cudaSuccess)
+    return BL_ERR_CUDA;
+  double host_energy = 0.0;
+  DevStatus host_status;
+  if (cudaMemcpyAsync(&host_energy, energy, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(&host_status, status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return BL_ERR_CUDA;
+  if (host_status.code != DEV_OK) return BL_ERR_DEVICE_TIMEOUT;
+  if (energy_out) *energy_out = host_energy;
+  return BL_OK;
+}

@@ -164,6 +164,29 @@ int bl_last_kernel_time(bl_ctx *ctx, const char *kernel, double *ms);
 /* Number of kernels this library launched since the context was created. */
 long long bl_kernel_launches(const bl_ctx *ctx);
 
+/* ---- allocation-free variant ------------------------------------------------ */
+
+/* No counterpart in the reference.  One minibatch iteration (as
+ * bl_minibatch_iteration) for callers that cannot allocate device memory while
+ * they run -- services that reserve all GPU memory up front in their own pool,
+ * real-time loops that forbid allocation after start-up, code enqueuing on a
+ * stream another component owns.  It allocates nothing: its scratch is a fixed
+ * 768 KiB device array inside the library, which limits batch to 256 and the
+ * launch to 160 blocks (larger requests return BL_ERR_TOO_LARGE).
+ * Device pointers, all caller-owned, on the current device:
+ *   d_rowptr[n+1], d_colids   neighbour lists the minibatch cursor matches
+ *                             (the CSR rows themselves when each row is sorted
+ *                             ascending without duplicates)
+ *   d_xy[2n] float32           coordinates, updated in place
+ *   d_force[2n], d_vertex_energy[n]  outputs: forces and |f|^2 per vertex
+ * stream: cudaStream_t (NULL = default stream); the call returns after the
+ * stream has finished it.  The first call on a device fetches the scratch
+ * array's device address: make it before any stream capture.  All calls on a
+ * device share the scratch, so calls that overlap on the GPU race. */
+int bl_minibatch_iteration_noalloc(int n, const int *d_rowptr, const int *d_colids, float *d_xy,
+                                   double *d_force, double *d_vertex_energy, int model, int batch,
+                                   double weight, double step, double *energy_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
