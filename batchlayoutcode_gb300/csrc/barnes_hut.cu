@@ -136,167 +136,140 @@ __global__ void morton_kernel(const float2 *__restrict__ pos, int n, u64 *keys, 
   vals[i] = i;
 }
 
-// ---- stable LSD radix sort, 8-bit digits, one kernel per digit pass -------
+// ---- stable LSD radix sort, 8-bit digits ------------------------------------
 //
-// Pass structure (decoupled look-back, after Adinets & Merrill, "Onesweep",
-// 2022): one kernel first counts all eight digit histograms; each pass then
-// takes tiles in launch order from an atomic counter, counts its tile's
-// digits, publishes those counts, ranks its keys stably, adds the counts of
-// the tiles before it (walking back until a tile that already published its
-// inclusive prefix) and scatters.  A tile that has published nothing yet is
-// waited for with a time bound; on timeout the pass records an error and the
-// waiting tile scatters nothing.
+// Each digit pass is three kernels without any inter-block waiting: the tile
+// digit counts (hist[d * ntiles + tile]), one block that turns every digit
+// row into exclusive offsets across tiles and scans the digit totals, and the
+// scatter, which ranks its tile's keys stably and writes them to
+// digit offset + row offset + rank.  Tiles are 4096 keys; warp w of a block
+// owns keys [w*512, (w+1)*512) of its tile and ranks them with warp-private
+// counters, so no block barrier sits inside the ranking loop.
 constexpr int kRsThreads = 256;
-constexpr int kRsItems = 16;
+constexpr int kRsItems = 4;
 constexpr int kRsTile = kRsThreads * kRsItems;
-constexpr unsigned int kFlagAgg = 1u << 30, kFlagInc = 2u << 30, kCountMask = (1u << 30) - 1u;
-constexpr unsigned long long kLookbackTimeoutNs = 2000000000ull;
+constexpr int kRsWarps = kRsThreads / 32;
 
-// digit histograms of all 8 passes: hist8[pass * 256 + digit]
-__global__ void __launch_bounds__(1024) rs_hist8_kernel(const u64 *__restrict__ keys, int n,
-                                                        unsigned int *hist8) {
-  __shared__ unsigned int h[8 * 256];
-  for (int k = threadIdx.x; k < 8 * 256; k += blockDim.x) h[k] = 0;
-  __syncthreads();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const u64 key = keys[i];
-#pragma unroll
-    for (int p = 0; p < 8; p++) atomicAdd(&h[p * 256 + (unsigned int)((key >> (8 * p)) & 255u)], 1u);
-  }
-  __syncthreads();
-  for (int k = threadIdx.x; k < 8 * 256; k += blockDim.x)
-    if (h[k]) atomicAdd(&hist8[k], h[k]);
-}
-
-// exclusive scan of each pass's 256 counts (block p scans pass p)
-__global__ void __launch_bounds__(256) rs_offsets_kernel(unsigned int *hist8) {
-  __shared__ unsigned int t[256];
-  unsigned int *row = hist8 + blockIdx.x * 256;
-  const unsigned int v = row[threadIdx.x];
-  t[threadIdx.x] = v;
-  __syncthreads();
-  for (int o = 1; o < 256; o <<= 1) {
-    const unsigned int y = (threadIdx.x >= (unsigned)o) ? t[threadIdx.x - o] : 0u;
-    __syncthreads();
-    t[threadIdx.x] += y;
-    __syncthreads();
-  }
-  row[threadIdx.x] = t[threadIdx.x] - v;
-}
-
-__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
-  unsigned int v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_u32(unsigned int *p, unsigned int v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-struct PassArgs {
-  const u64 *kin;
-  const int *vin;
-  u64 *kout;
-  int *vout;
-  int n, shift, ntiles;
-  const unsigned int *digit_off;  // 256 exclusive offsets of this pass
-  unsigned int *lookback;         // [ntiles][256] flag|count, zeroed before the pass
-  unsigned int *tile_counter;     // zeroed before the pass
-  DevStatus *st;
-};
-
-__global__ void __launch_bounds__(kRsThreads) rs_pass_kernel(PassArgs a) {
-  __shared__ unsigned int s_tile;
-  __shared__ unsigned int s_cnt[256];
-  __shared__ unsigned int s_run[256];
-  __shared__ unsigned int s_w[kRsThreads / 32][256];
-  __shared__ unsigned int s_base[256];
-  __shared__ int s_abort;
+__global__ void __launch_bounds__(kRsThreads) rs_count_kernel(const u64 *__restrict__ keys, int n, int shift,
+                                                              int ntiles, unsigned int *hist) {
+  __shared__ unsigned int cnt[kRsWarps][256];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  if (tid == 0) {
-    s_tile = atomicAdd(a.tile_counter, 1u);
-    s_abort = 0;
-  }
-  s_cnt[tid] = 0;
-  s_run[tid] = 0;
-  __syncthreads();
-  const int tile = (int)s_tile;
-  const int base = tile * kRsTile;
-  u64 key[kRsItems];
-  unsigned int dig[kRsItems];
 #pragma unroll
+  for (int w = 0; w < kRsWarps; w++) cnt[w][tid] = 0;
+  __syncthreads();
+  const int wbase = blockIdx.x * kRsTile + warp * (kRsItems * 32);
+#pragma unroll 4
   for (int r = 0; r < kRsItems; r++) {
-    const int idx = base + r * kRsThreads + tid;
-    key[r] = (idx < a.n) ? a.kin[idx] : 0ull;
-    dig[r] = (idx < a.n) ? ((unsigned int)(key[r] >> a.shift) & 255u) : 256u;
-    if (dig[r] < 256u) atomicAdd(&s_cnt[dig[r]], 1u);
+    const int idx = wbase + r * 32 + lane;
+    if (idx < n) atomicAdd(&cnt[warp][(unsigned int)(keys[idx] >> shift) & 255u], 1u);
   }
   __syncthreads();
-  // publish this tile's counts as soon as they are known
-  unsigned int *my = a.lookback + (size_t)tile * 256;
-  if (tile == 0) st_release_u32(&my[tid], kFlagInc | s_cnt[tid]);
-  else st_release_u32(&my[tid], kFlagAgg | s_cnt[tid]);
-  // stable local ranks, one round of 256 keys at a time
-  unsigned int rank[kRsItems];
+  unsigned int tot = 0;
+#pragma unroll
+  for (int w = 0; w < kRsWarps; w++) tot += cnt[w][tid];
+  hist[(size_t)tid * ntiles + blockIdx.x] = tot;
+}
+
+// Block d turns digit row d (ntiles contiguous counts) into exclusive
+// offsets across tiles, 256 tiles at a time, and stores the row total.
+__global__ void __launch_bounds__(256) rs_rowscan_kernel(unsigned int *hist, int ntiles,
+                                                         unsigned int *row_total) {
+  __shared__ unsigned int ws[8];
+  __shared__ unsigned int carry;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  unsigned int *row = hist + (size_t)blockIdx.x * ntiles;
+  if (tid == 0) carry = 0;
+  __syncthreads();
+  for (int c0 = 0; c0 < ntiles; c0 += 256) {
+    const int b = c0 + tid;
+    const unsigned int v = (b < ntiles) ? row[b] : 0u;
+    unsigned int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    unsigned int wpre = 0, total = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const unsigned int t = ws[k];
+      if (k < w) wpre += t;
+      total += t;
+    }
+    const unsigned int base = carry;
+    if (b < ntiles) row[b] = base + wpre + x - v;
+    __syncthreads();
+    if (tid == 0) carry = base + total;
+    __syncthreads();
+  }
+  if (tid == 0) row_total[blockIdx.x] = carry;
+}
+
+__global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
+    const u64 *__restrict__ kin, const int *__restrict__ vin, u64 *__restrict__ kout, int *__restrict__ vout,
+    int n, int shift, int ntiles, const unsigned int *__restrict__ hist, const unsigned int *__restrict__ row_total) {
+  __shared__ unsigned int s_cnt[kRsWarps][256];  // per-warp counts, then per-warp offsets
+  __shared__ unsigned int s_base[256];
+  __shared__ unsigned int s_ws[kRsWarps];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+#pragma unroll
+  for (int w = 0; w < kRsWarps; w++) s_cnt[w][tid] = 0;
+  {
+    // digit offset = exclusive scan of the 256 row totals (every block does it)
+    const unsigned int v = row_total[tid];
+    unsigned int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_ws[warp] = x;
+    __syncthreads();
+    unsigned int wpre = 0;
+#pragma unroll
+    for (int k = 0; k < kRsWarps; k++)
+      if (k < warp) wpre += s_ws[k];
+    s_base[tid] = wpre + x - v + hist[(size_t)tid * ntiles + blockIdx.x];
+  }
+  __syncthreads();
+  const int wbase = blockIdx.x * kRsTile + warp * (kRsItems * 32);
   const unsigned int lt = (1u << lane) - 1u;
+  u64 key[kRsItems];
+  unsigned int rd[kRsItems];  // rank within the warp's keys (low 16 bits) | digit << 16, digit 256 = none
 #pragma unroll
   for (int r = 0; r < kRsItems; r++) {
-#pragma unroll
-    for (int w = 0; w < kRsThreads / 32; w++) s_w[w][tid] = 0;
-    __syncthreads();
-    const unsigned int peers = __match_any_sync(0xffffffffu, dig[r]);
-    const unsigned int rk = __popc(peers & lt);
-    if (dig[r] < 256u && rk == 0) s_w[warp][dig[r]] = __popc(peers);
-    __syncthreads();
-    {
-      unsigned int run = s_run[tid];
-#pragma unroll
-      for (int w = 0; w < kRsThreads / 32; w++) {
-        const unsigned int c = s_w[w][tid];
-        s_w[w][tid] = run;
-        run += c;
-      }
-      s_run[tid] = run;
-    }
-    __syncthreads();
-    rank[r] = (dig[r] < 256u) ? s_w[warp][dig[r]] + rk : 0u;
-    __syncthreads();  // s_w is cleared at the top of the next round
+    const int idx = wbase + r * 32 + lane;
+    const bool valid = idx < n;
+    key[r] = valid ? kin[idx] : 0ull;
+    const unsigned int d = valid ? ((unsigned int)(key[r] >> shift) & 255u) : 256u;
+    const unsigned int peers = __match_any_sync(0xffffffffu, d);
+    const unsigned int leader = __ffs(peers) - 1;
+    unsigned int old = 0;
+    if (d < 256u) old = s_cnt[warp][d];
+    __syncwarp();
+    if (d < 256u && lane == leader) s_cnt[warp][d] = old + __popc(peers);
+    __syncwarp();
+    rd[r] = (old + __popc(peers & lt)) | (d << 16);
   }
-  // look back for the exclusive prefix of digit `tid` over earlier tiles
-  unsigned int excl = 0;
-  if (tile > 0) {
-    int t = tile - 1;
-    const unsigned long long t0 = dev_globaltimer();
-    while (t >= 0) {
-      const unsigned int v = ld_acquire_u32(&a.lookback[(size_t)t * 256 + tid]);
-      if (v & kFlagInc) {
-        excl += v & kCountMask;
-        break;
-      }
-      if (v & kFlagAgg) {
-        excl += v & kCountMask;
-        t--;
-        continue;
-      }
-      if (dev_globaltimer() - t0 > kLookbackTimeoutNs) {
-        dev_record_error(a.st, DEV_TIMEOUT_TREE);
-        s_abort = 1;
-        break;
-      }
-    }
-    st_release_u32(&my[tid], kFlagInc | (excl + s_cnt[tid]));
-  }
-  s_base[tid] = a.digit_off[tid] + excl;
   __syncthreads();
-  if (s_abort) return;
+  unsigned int run = 0;
+#pragma unroll
+  for (int w = 0; w < kRsWarps; w++) {
+    const unsigned int c = s_cnt[w][tid];
+    s_cnt[w][tid] = run;
+    run += c;
+  }
+  __syncthreads();
 #pragma unroll
   for (int r = 0; r < kRsItems; r++) {
-    if (dig[r] < 256u) {
-      const int idx = base + r * kRsThreads + tid;
-      const unsigned int p = s_base[dig[r]] + rank[r];
-      if (p < (unsigned int)a.n) {
-        a.kout[p] = key[r];
-        a.vout[p] = a.vin[idx];
+    const unsigned int d = rd[r] >> 16;
+    if (d < 256u) {
+      const unsigned int p = s_base[d] + s_cnt[warp][d] + (rd[r] & 0xffffu);
+      if (p < (unsigned int)n) {
+        kout[p] = key[r];
+        vout[p] = vin[wbase + r * 32 + lane];
       }
     }
   }
@@ -686,14 +659,23 @@ __global__ void __launch_bounds__(256) traverse_kernel(TraverseArgs a) {
     const int batch_lo = (v / a.batch) * a.batch;
     float hx = -fx, lx = 0.f, hy = -fy, ly = 0.f;
     const int e1 = a.rowptr[v + 1];
-    for (int e = a.rowptr[v]; e < e1; e++) {
-      const int j = a.colids[e];
-      if (j < batch_lo) continue;
-      const float2 pj = a.pold[j];
-      const float dx = pj.x - pv.x, dy = pj.y - pv.y;
-      const float sc = a.W * sqrtf(fmaf(dx, dx, dy * dy));
-      ff_add(hx, lx, dx * sc);
-      ff_add(hy, ly, dy * sc);
+    constexpr int kU = 4;  // index loads first, then position loads, then the ordered sum
+    for (int e = a.rowptr[v]; e < e1; e += kU) {
+      int j[kU];
+      float2 pj[kU];
+#pragma unroll
+      for (int u = 0; u < kU; u++) j[u] = (e + u < e1) ? a.colids[e + u] : -1;
+#pragma unroll
+      for (int u = 0; u < kU; u++)
+        if (j[u] >= batch_lo) pj[u] = a.pold[j[u]];
+#pragma unroll
+      for (int u = 0; u < kU; u++) {
+        if (j[u] < batch_lo) continue;  // moved earlier in this iteration, or past the row end
+        const float dx = pj[u].x - pv.x, dy = pj[u].y - pv.y;
+        const float sc = a.W * sqrtf(fmaf(dx, dx, dy * dy));
+        ff_add(hx, lx, dx * sc);
+        ff_add(hy, ly, dy * sc);
+      }
     }
     a.f0[v] = make_float4(hx, hy, lx, ly);
   }
@@ -788,7 +770,7 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   fr(s.qbelow); fr(s.startcnt); fr(s.startbase); fr(s.nodes); fr(s.nodes_c64);
   fr(s.nodes_lvl); fr(s.rep); fr(s.f0); fr(s.pos_alt);
   const size_t nb = (n + kRsTile - 1) / kRsTile;
-  s.hist_entries = 8 * 256 + 8 + 8 * 256 * std::max<size_t>(nb, 1);
+  s.hist_entries = 256 * std::max<size_t>(nb, 1) + 256;
   const size_t m = std::max<size_t>(n, 2);
   BL_CUDA(ctx, cudaMalloc(&s.keys, m * 8));
   BL_CUDA(ctx, cudaMalloc(&s.keys_alt, m * 8));
@@ -833,30 +815,16 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   const int nb = nblk(n, kRsTile);
   unsigned long long *kin = s.keys, *kout = s.keys_alt;
   int *vin = s.perm, *vout = s.perm_alt;
-  // hist layout: [8 passes x 256 digit offsets][8 tile counters][8 x ntiles x 256 look-back]
-  unsigned int *hist8 = s.hist, *counters = s.hist + 8 * 256, *lookback = s.hist + 8 * 256 + 8;
+  // hist layout: [256 digits x ntiles counts][256 digit-row totals]
+  unsigned int *digit_off = s.hist + (size_t)256 * nb;
   bl_time_begin(ctx, "radix_sort");
-  BL_CUDA(ctx, cudaMemsetAsync(s.hist, 0, (8 * 256 + 8 + (size_t)8 * nb * 256) * sizeof(unsigned int), st));
-  rs_hist8_kernel<<<ctx->num_sms, 1024, 0, st>>>(kin, n, hist8);
-  rs_offsets_kernel<<<8, 256, 0, st>>>(hist8);
-  ctx->launches += 2;
   for (int pass = 0; pass < 8; pass++) {
-    PassArgs pa;
-    pa.kin = kin;
-    pa.vin = vin;
-    pa.kout = kout;
-    pa.vout = vout;
-    pa.n = n;
-    pa.shift = 8 * pass;
-    pa.ntiles = nb;
-    pa.digit_off = hist8 + pass * 256;
-    pa.lookback = lookback + (size_t)pass * nb * 256;
-    pa.tile_counter = counters + pass;
-    pa.st = s.status;
-    rs_pass_kernel<<<nb, kRsThreads, 0, st>>>(pa);
+    rs_count_kernel<<<nb, kRsThreads, 0, st>>>(kin, n, 8 * pass, nb, s.hist);
+    rs_rowscan_kernel<<<256, 256, 0, st>>>(s.hist, nb, digit_off);
+    rs_scatter_kernel<<<nb, kRsThreads, 0, st>>>(kin, vin, kout, vout, n, 8 * pass, nb, s.hist, digit_off);
     std::swap(kin, kout);
     std::swap(vin, vout);
-    ctx->launches++;
+    ctx->launches += 3;
   }
   bl_time_end(ctx, "radix_sort");
   // 8 passes: sorted data is back in keys/perm

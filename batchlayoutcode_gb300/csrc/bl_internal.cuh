@@ -63,18 +63,19 @@ __device__ __forceinline__ bool grid_barrier(DevStatus *st, unsigned int &epoch)
     atomicAdd(&st->barrier, 1u);
     const unsigned int target = epoch * gridDim.x;
     const unsigned long long t0 = dev_globaltimer();
-    unsigned int ok = 1;
+    unsigned int ok = 1, polls = 0;
     while (ld_acquire_gpu(&st->barrier) < target) {
-      if (ld_volatile_u32(&st->code) != 0u) {
-        ok = 0;
-        break;
+      if ((++polls & 127u) == 0u) {
+        if (ld_volatile_u32(&st->code) != 0u) {
+          ok = 0;
+          break;
+        }
+        if (dev_globaltimer() - t0 > kBarrierTimeoutNs) {
+          dev_record_error(st, DEV_TIMEOUT_GRID_BARRIER);
+          ok = 0;
+          break;
+        }
       }
-      if (dev_globaltimer() - t0 > kBarrierTimeoutNs) {
-        dev_record_error(st, DEV_TIMEOUT_GRID_BARRIER);
-        ok = 0;
-        break;
-      }
-      __nanosleep(32);
     }
     if (ld_volatile_u32(&st->code) != 0u) ok = 0;
     s_ok = ok;
@@ -139,6 +140,8 @@ struct Scratch {
   // minibatch sweep
   float2 *partials = nullptr;
   size_t partials_bytes = 0;
+  int *cursor = nullptr;  // per (block, vertex) neighbour cursor start
+  int cursor_grid = 0;
   // Barnes-Hut
   size_t bh_n = 0;
   unsigned long long *keys = nullptr, *keys_alt = nullptr;

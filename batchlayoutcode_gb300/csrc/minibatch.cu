@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <climits>
 #include <cmath>
 #include <mutex>
 
@@ -47,6 +48,9 @@ struct MinibatchArgs {
   int n, batch, nbatches, model, grid;
   double W;
   const int *eff_rowptr, *eff_colids;
+  // cursor[s * n + i]: neighbours of i below the first vertex of block s's
+  // slice (null: found by binary search)
+  const int *cursor;
   float2 *pos;
   double2 *force;
   double *e;
@@ -69,6 +73,71 @@ __device__ __forceinline__ void rep_pair(float xs, float ys, float xi, float yi,
   const float r = rcp_approx(d2);
   fx = fmaf(-dx, r, fx);
   fy = fmaf(-dy, r, fy);
+}
+
+// Attraction of a matched neighbour, FP32 (algorithms.cpp:759 FR, :912 LinLog, :985 FA).
+__device__ __forceinline__ void attract_pair(int model, float W, float xs, float ys, float xi, float yi,
+                                             float &fx, float &fy) {
+  const float dx = xs - xi, dy = ys - yi;
+  float sc;
+  if (model == MODEL_FR) sc = W * sqrtf(fmaf(dx, dx, dy * dy));
+  else if (model == MODEL_LINLOG) sc = log2f(1.0f + W * sqrtf(fmaf(dx, dx, dy * dy)));
+  else sc = W;
+  fx = fmaf(dx, sc, fx);
+  fy = fmaf(dy, sc, fy);
+}
+
+// Next neighbour of target i at or after global index `from`, as an index
+// local to the slice (INT_MAX when none): the reference's kindex cursor
+// (algorithms.cpp:746,758-762) positioned at this block's part of the sweep.
+struct Cursor {
+  int k, kend, next;
+};
+
+__device__ __forceinline__ void cursor_seek(Cursor &c, const int *__restrict__ colids, int from, int sbase) {
+  // bounded: at most the neighbours between the two slice starts
+  while (c.k < c.kend && __ldg(&colids[c.k]) < from) c.k++;
+  c.next = (c.k < c.kend) ? __ldg(&colids[c.k]) - sbase : INT_MAX;
+}
+
+__device__ __forceinline__ void cursor_init(Cursor &c, const MinibatchArgs &a, int s, int i, int slo, int from,
+                                            int sbase) {
+  c.k = a.eff_rowptr[i];
+  c.kend = a.eff_rowptr[i + 1];
+  if (a.cursor) {
+    c.k += a.cursor[(size_t)s * a.n + i];
+  } else {  // lower bound of slo in the sorted neighbour list
+    int lo = c.k, hi = c.kend;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (__ldg(&a.eff_colids[mid]) < slo) lo = mid + 1;
+      else hi = mid;
+    }
+    c.k = lo;
+  }
+  cursor_seek(c, a.eff_colids, from, sbase);
+}
+
+// One source q (slice-local) against one target: attraction and cursor
+// advance when q is the target's next neighbour, repulsion otherwise.
+__device__ __forceinline__ void pair_exact(const MinibatchArgs &a, Cursor &c, int q, float xs, float ys,
+                                           float xi, float yi, int sbase, float &fx, float &fy) {
+  if (q == c.next) {
+    attract_pair(a.model, (float)a.W, xs, ys, xi, yi, fx, fy);
+    c.k++;
+    c.next = (c.k < c.kend) ? __ldg(&a.eff_colids[c.k]) - sbase : INT_MAX;
+  } else {
+    rep_pair(xs, ys, xi, yi, fx, fy);
+  }
+}
+
+// Compensated float-float accumulation (Knuth's TwoSum).
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float t) {
+  const float sum = hi + t;
+  const float bb = sum - hi;
+  const float err = (hi - (sum - bb)) + (t - bb);
+  hi = sum;
+  lo += err;
 }
 
 // Slice of sources owned by block s: [lo, hi).
@@ -139,32 +208,47 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
       const int buf = c & 1;
       for (int t = tid; t < cnt; t += kThreads) tpos[t] = a.pos[base + t];
       __syncthreads();
-      // ---- sweep: partial repulsion of this block's slice on every target ----
+      // ---- sweep: partial force of this block's slice on every target ----
+      // repulsion for every source, attraction instead for the target's
+      // matched neighbours (found by a sorted cursor, rare), as in the
+      // reference's j loop
       for (int c0 = 0; c0 < cnt; c0 += kChunk) {
         const int t0 = c0 + gl, t1 = t0 + kGroup;
-        const float2 p0 = (t0 < cnt) ? tpos[t0] : make_float2(0.f, 0.f);
-        const float2 p1 = (t1 < cnt) ? tpos[t1] : make_float2(0.f, 0.f);
+        const bool v0 = t0 < cnt, v1 = t1 < cnt;
+        const float2 p0 = v0 ? tpos[t0] : make_float2(0.f, 0.f);
+        const float2 p1 = v1 ? tpos[t1] : make_float2(0.f, 0.f);
+        Cursor c0r, c1r;
+        c0r.next = c1r.next = INT_MAX;
+        if (v0) cursor_init(c0r, a, s, base + t0, slo, sbase + ga, sbase);
+        if (v1) cursor_init(c1r, a, s, base + t1, slo, sbase + ga, sbase);
         float fx0a = 0.f, fy0a = 0.f, fx0b = 0.f, fy0b = 0.f;
         float fx1a = 0.f, fy1a = 0.f, fx1b = 0.f, fy1b = 0.f;
         int k = ga;
         if ((k & 1) && k < gb) {
           const float2 q = slice[k];
-          rep_pair(q.x, q.y, p0.x, p0.y, fx0a, fy0a);
-          rep_pair(q.x, q.y, p1.x, p1.y, fx1a, fy1a);
+          pair_exact(a, c0r, k, q.x, q.y, p0.x, p0.y, sbase, fx0a, fy0a);
+          pair_exact(a, c1r, k, q.x, q.y, p1.x, p1.y, sbase, fx1a, fy1a);
           k++;
         }
 #pragma unroll 4
         for (; k + 1 < gb; k += 2) {
           const float4 q = *reinterpret_cast<const float4 *>(&slice[k]);
-          rep_pair(q.x, q.y, p0.x, p0.y, fx0a, fy0a);
-          rep_pair(q.z, q.w, p0.x, p0.y, fx0b, fy0b);
-          rep_pair(q.x, q.y, p1.x, p1.y, fx1a, fy1a);
-          rep_pair(q.z, q.w, p1.x, p1.y, fx1b, fy1b);
+          if (c0r.next > k + 1 && c1r.next > k + 1) {
+            rep_pair(q.x, q.y, p0.x, p0.y, fx0a, fy0a);
+            rep_pair(q.z, q.w, p0.x, p0.y, fx0b, fy0b);
+            rep_pair(q.x, q.y, p1.x, p1.y, fx1a, fy1a);
+            rep_pair(q.z, q.w, p1.x, p1.y, fx1b, fy1b);
+          } else {
+            pair_exact(a, c0r, k, q.x, q.y, p0.x, p0.y, sbase, fx0a, fy0a);
+            pair_exact(a, c0r, k + 1, q.z, q.w, p0.x, p0.y, sbase, fx0b, fy0b);
+            pair_exact(a, c1r, k, q.x, q.y, p1.x, p1.y, sbase, fx1a, fy1a);
+            pair_exact(a, c1r, k + 1, q.z, q.w, p1.x, p1.y, sbase, fx1b, fy1b);
+          }
         }
         if (k < gb) {
           const float2 q = slice[k];
-          rep_pair(q.x, q.y, p0.x, p0.y, fx0b, fy0b);
-          rep_pair(q.x, q.y, p1.x, p1.y, fx1b, fy1b);
+          pair_exact(a, c0r, k, q.x, q.y, p0.x, p0.y, sbase, fx0b, fy0b);
+          pair_exact(a, c1r, k, q.x, q.y, p1.x, p1.y, sbase, fx1b, fy1b);
         }
         const float2 r0 = make_float2(fx0a + fx0b, fy0a + fy0b);
         const float2 r1 = make_float2(fx1a + fx1b, fy1a + fy1b);
@@ -189,61 +273,50 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
       }
       ok = grid_barrier(a.st, epoch);
       if (!ok) break;
-      // ---- owners: reduce partials, neighbour correction, update ------------
+      // ---- owners: sum the partials (float-float, fixed order), update -------
       const int olo = max(slo, base), ohi = min(shi, base + cnt);
       if (olo < ohi) {
         const float2 *P = a.partials + (size_t)buf * a.batch * a.grid;
+        const float stepf = (float)step;
         for (int i = olo + warp; i < ohi; i += kWarps) {
           const int t = i - base;
-          double fx = 0.0, fy = 0.0;
+          float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f;
           for (int q = lane; q < a.grid; q += 32) {
             const float2 v = __ldcg(&P[(size_t)t * a.grid + q]);
-            fx += (double)v.x;
-            fy += (double)v.y;
-          }
-          const float2 pi = tpos[t];
-          double cx = 0.0, cy = 0.0;
-          const int k0 = a.eff_rowptr[i], k1 = a.eff_rowptr[i + 1];
-          for (int k = k0 + lane; k < k1; k += 32) {
-            const int j = a.eff_colids[k];
-            const float2 pj = (j >= base && j < base + cnt) ? tpos[j - base] : __ldcg(&a.pos[j]);
-            const float dx = pj.x - pi.x, dy = pj.y - pi.y;
-            // the sweep added -d/|d|^2 for this pair: take it back
-            const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
-            const float r = rcp_approx(d2);
-            float ax, ay;
-            if (a.model == MODEL_FR) {
-              const float sc = (float)a.W * sqrtf(dx * dx + dy * dy);
-              ax = dx * sc; ay = dy * sc;
-            } else if (a.model == MODEL_LINLOG) {
-              const float sc = log2f(1.0f + (float)a.W * sqrtf(dx * dx + dy * dy));
-              ax = dx * sc; ay = dy * sc;
-            } else {
-              ax = dx * (float)a.W; ay = dy * (float)a.W;
-            }
-            cx += (double)ax + (double)(dx * r);
-            cy += (double)ay + (double)(dy * r);
+            ff_add(hx, lx, v.x);
+            ff_add(hy, ly, v.y);
           }
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) {
-            fx += __shfl_xor_sync(0xffffffffu, fx, o);
-            fy += __shfl_xor_sync(0xffffffffu, fy, o);
-            cx += __shfl_xor_sync(0xffffffffu, cx, o);
-            cy += __shfl_xor_sync(0xffffffffu, cy, o);
+            const float ohx = __shfl_xor_sync(0xffffffffu, hx, o);
+            const float olx = __shfl_xor_sync(0xffffffffu, lx, o);
+            const float ohy = __shfl_xor_sync(0xffffffffu, hy, o);
+            const float oly = __shfl_xor_sync(0xffffffffu, ly, o);
+            ff_add(hx, lx, ohx);
+            lx += olx;
+            ff_add(hy, ly, ohy);
+            ly += oly;
           }
           if (lane == 0) {
-            fx += cx;
-            fy += cy;
-            const double mag = sqrt(fx * fx + fy * fy);
+            const float2 pi = tpos[t];
+            const float fx = hx + lx, fy = hy + ly;
             float2 np = pi;
-            if (mag > 0.0) {
-              np.x = (float)((double)pi.x + (fx / mag) * step);
-              np.y = (float)((double)pi.y + (fy / mag) * step);
+            const float m2 = fmaf(fx, fx, fy * fy);
+            if (m2 >= 1.17549435e-38f && m2 <= 3.0e38f) {
+              const float rm = rsqrt_approx(m2);
+              np.x = fmaf(stepf, fx * rm, pi.x);
+              np.y = fmaf(stepf, fy * rm, pi.y);
+            } else if (fx != 0.f || fy != 0.f) {  // |f|^2 outside the FP32 range
+              const double dfx = (double)hx + (double)lx, dfy = (double)hy + (double)ly;
+              const double mag = sqrt(dfx * dfx + dfy * dfy);
+              np.x = (float)((double)pi.x + (dfx / mag) * step);
+              np.y = (float)((double)pi.y + (dfy / mag) * step);
             }
             a.pos[i] = np;
             slice[i - sbase] = np;
-            a.force[i] = make_double2(fx, fy);
-            a.e[i] = fx * fx + fy * fy;
+            const double dfx = (double)hx + (double)lx, dfy = (double)hy + (double)ly;
+            a.force[i] = make_double2(dfx, dfy);
+            a.e[i] = dfx * dfx + dfy * dfy;
           }
         }
       }
@@ -276,6 +349,24 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
     loop++;
   }
   if (s == 0 && tid == 0) *a.loops = loop;
+}
+
+// cursor[s * n + i] = number of matched neighbours of i below slice_lo(s)
+__global__ void cursor_table_kernel(const int *__restrict__ rowptr, const int *__restrict__ colids, int n,
+                                    int grid, int *cursor) {
+  const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= (long long)n * grid) return;
+  const int s = (int)(gid / n), i = (int)(gid % n);
+  int slo, shi;
+  slice_of(n, grid, s, slo, shi);
+  int lo = rowptr[i], hi = rowptr[i + 1];
+  const int k0 = lo;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (colids[mid] < slo) lo = mid + 1;
+    else hi = mid;
+  }
+  cursor[gid] = lo - k0;
 }
 
 }  // namespace
@@ -323,6 +414,19 @@ int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step
   if (occ < 1 || grid > occ * ctx->num_sms)
     return bl_fail(ctx, -5, "minibatch kernel cannot be co-resident");
   if (int rc = ensure_minibatch_scratch(ctx, batch, grid)) return rc;
+  if (ctx->s.cursor_grid != grid) {
+    if (ctx->s.cursor) cudaFree(ctx->s.cursor);
+    ctx->s.cursor = nullptr;
+    ctx->s.cursor_grid = 0;
+    BL_CUDA(ctx, cudaMalloc(&ctx->s.cursor, (size_t)n * grid * sizeof(int)));
+    const long long total = (long long)n * grid;
+    cursor_table_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(ctx->g.eff_rowptr,
+                                                                                ctx->g.eff_colids, n, grid,
+                                                                                ctx->s.cursor);
+    BL_CUDA(ctx, cudaGetLastError());
+    ctx->launches++;
+    ctx->s.cursor_grid = grid;
+  }
   BL_CUDA(ctx, cudaMemsetAsync(ctx->s.status, 0, sizeof(DevStatus), ctx->stream));
 
   MinibatchArgs a;
@@ -334,6 +438,7 @@ int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step
   a.W = ctx->weight;
   a.eff_rowptr = ctx->g.eff_rowptr;
   a.eff_colids = ctx->g.eff_colids;
+  a.cursor = ctx->s.cursor;
   a.pos = ctx->pos;
   a.force = ctx->force;
   a.e = ctx->e;
@@ -469,6 +574,7 @@ extern "C" int bl_minibatch_iteration_noalloc(int n, const int *d_rowptr, const 
   a.W = weight;
   a.eff_rowptr = d_rowptr;
   a.eff_colids = d_colids;
+  a.cursor = nullptr;
   a.pos = reinterpret_cast<float2 *>(d_xy);
   a.force = reinterpret_cast<double2 *>(d_force);
   a.e = d_vertex_energy;
