@@ -35,6 +35,7 @@ int bl_check_status(bl_ctx *ctx) {
   if (st.code == DEV_OK) return 0;
   const char *what = st.code == DEV_TIMEOUT_GRID_BARRIER ? "grid barrier timed out"
                      : st.code == DEV_TIMEOUT_TREE        ? "tree build wait timed out"
+                     : st.code == DEV_FORCE_RANGE         ? "force beyond the fixed-point range (coincident vertices?)"
                                                           : "device error";
   cudaMemset(ctx->s.status, 0, sizeof(DevStatus));
   return bl_fail(ctx, BL_ERR_DEVICE_TIMEOUT,

@@ -18,6 +18,7 @@ enum : unsigned int {
   DEV_TIMEOUT_GRID_BARRIER = 1,
   DEV_TIMEOUT_TREE = 2,
   DEV_BAD_INDEX = 3,
+  DEV_FORCE_RANGE = 4,
 };
 
 struct DevStatus {

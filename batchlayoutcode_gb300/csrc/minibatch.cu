@@ -44,6 +44,23 @@ constexpr int kChunk = 2 * kGroup;             // 256 targets per sweep pass
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxBatch = 4096;
 
+// Block partial forces are summed across blocks as 64-bit fixed-point
+// integers (units of 2^-28): integer addition is exact and associative, so
+// the total does not depend on the order of the atomics and stays
+// deterministic.  A partial beyond +-2^34 (forces of ~1e10, coincident
+// vertices) is reported as an error instead of wrapping.
+constexpr float kFixScale = 268435456.0f;        // 2^28
+constexpr double kFixInv = 1.0 / 268435456.0;    // 2^-28
+constexpr float kFixLimit = 17179869184.0f;      // 2^34
+
+__device__ __forceinline__ void acc_add(long long *dst, float v, DevStatus *st) {
+  if (!(fabsf(v) < kFixLimit)) {
+    dev_record_error(st, DEV_FORCE_RANGE);
+    return;
+  }
+  atomicAdd(reinterpret_cast<unsigned long long *>(dst), (unsigned long long)__float2ll_rn(v * kFixScale));
+}
+
 struct MinibatchArgs {
   int n, batch, nbatches, model, grid;
   double W;
@@ -54,7 +71,7 @@ struct MinibatchArgs {
   float2 *pos;
   double2 *force;
   double *e;
-  float2 *partials;       // [2][batch][grid]
+  long long *acc;         // [2][batch][2] fixed-point force sums (2^-28 units)
   double *energy;         // energy per iteration (device)
   double *energy_parts;   // [grid]
   long long *loops;       // iterations run (device, 1 value)
@@ -87,47 +104,97 @@ __device__ __forceinline__ void attract_pair(int model, float W, float xs, float
   fy = fmaf(dy, sc, fy);
 }
 
-// Next neighbour of target i at or after global index `from`, as an index
-// local to the slice (INT_MAX when none): the reference's kindex cursor
-// (algorithms.cpp:746,758-762) positioned at this block's part of the sweep.
-struct Cursor {
-  int k, kend, next;
+// The reference's kindex cursor (algorithms.cpp:746,758-762) restricted to
+// this block's slice: the target's matched neighbours inside [slo, shi) are
+// staged in shared memory (up to kNbCap, slice-local indices) with the
+// batch's targets, so stepping the cursor reads shared memory; a target with
+// more neighbours in the slice continues from global memory.
+constexpr int kNbCap = 16;
+
+struct NbList {
+  int *ids;    // [kChunk][kNbCap] slice-local ids
+  int *meta;   // [kChunk][2]: number of neighbours in the slice, first CSR index
 };
 
-__device__ __forceinline__ void cursor_seek(Cursor &c, const int *__restrict__ colids, int from, int sbase) {
-  // bounded: at most the neighbours between the two slice starts
-  while (c.k < c.kend && __ldg(&colids[c.k]) < from) c.k++;
-  c.next = (c.k < c.kend) ? __ldg(&colids[c.k]) - sbase : INT_MAX;
-}
-
-__device__ __forceinline__ void cursor_init(Cursor &c, const MinibatchArgs &a, int s, int i, int slo, int from,
-                                            int sbase) {
-  c.k = a.eff_rowptr[i];
-  c.kend = a.eff_rowptr[i + 1];
-  if (a.cursor) {
-    c.k += a.cursor[(size_t)s * a.n + i];
-  } else {  // lower bound of slo in the sorted neighbour list
-    int lo = c.k, hi = c.kend;
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (__ldg(&a.eff_colids[mid]) < slo) lo = mid + 1;
-      else hi = mid;
+// Stage the neighbours of targets [base, base + cnt) (cnt <= kChunk) that lie
+// in [slo, shi).  One thread per target.
+__device__ __forceinline__ void stage_neighbours(const MinibatchArgs &a, NbList L, int s, int base, int cnt,
+                                                 int slo, int shi, int sbase) {
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const int i = base + t;
+    const int r0 = a.eff_rowptr[i], r1 = a.eff_rowptr[i + 1];
+    int k0, k1;
+    if (a.cursor) {
+      k0 = r0 + a.cursor[(size_t)s * a.n + i];
+      k1 = (s + 1 < a.grid) ? r0 + a.cursor[(size_t)(s + 1) * a.n + i] : r1;
+    } else {  // lower bounds of slo and shi in the sorted neighbour list
+      int lo = r0, hi = r1;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&a.eff_colids[mid]) < slo) lo = mid + 1;
+        else hi = mid;
+      }
+      k0 = lo;
+      hi = r1;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&a.eff_colids[mid]) < shi) lo = mid + 1;
+        else hi = mid;
+      }
+      k1 = lo;
     }
-    c.k = lo;
+    const int m = min(k1 - k0, kNbCap);
+    for (int q = 0; q < m; q++) L.ids[t * kNbCap + q] = __ldg(&a.eff_colids[k0 + q]) - sbase;
+    L.meta[2 * t] = k1 - k0;
+    L.meta[2 * t + 1] = k0;
   }
-  cursor_seek(c, a.eff_colids, from, sbase);
 }
 
-// One source q (slice-local) against one target: attraction and cursor
-// advance when q is the target's next neighbour, repulsion otherwise.
-__device__ __forceinline__ void pair_exact(const MinibatchArgs &a, Cursor &c, int q, float xs, float ys,
-                                           float xi, float yi, int sbase, float &fx, float &fy) {
-  if (q == c.next) {
-    attract_pair(a.model, (float)a.W, xs, ys, xi, yi, fx, fy);
-    c.k++;
-    c.next = (c.k < c.kend) ? __ldg(&a.eff_colids[c.k]) - sbase : INT_MAX;
-  } else {
-    rep_pair(xs, ys, xi, yi, fx, fy);
+struct Cursor {
+  int ptr, cnt, k0, next;
+  const int *ids;
+};
+
+__device__ __forceinline__ int cursor_at(const MinibatchArgs &a, const Cursor &c, int sbase) {
+  if (c.ptr >= c.cnt) return INT_MAX;
+  if (c.ptr < kNbCap) return c.ids[c.ptr];
+  return __ldg(&a.eff_colids[c.k0 + c.ptr]) - sbase;  // beyond the staged ones
+}
+
+// Cursor of target t positioned at the group's first source `from` (slice-local).
+__device__ __forceinline__ void cursor_init(Cursor &c, const MinibatchArgs &a, NbList L, int t, int from,
+                                            int sbase) {
+  c.ids = L.ids + t * kNbCap;
+  c.cnt = L.meta[2 * t];
+  c.k0 = L.meta[2 * t + 1];
+  c.ptr = 0;
+  c.next = cursor_at(a, c, sbase);
+  // bounded by the neighbours inside the slice
+  while (c.next < from) {
+    c.ptr++;
+    c.next = cursor_at(a, c, sbase);
+  }
+}
+
+// For each matched neighbour q of the target with ga <= q < gb: remove the
+// repulsion the sweep added (identical FP32 operations) and add the model's
+// attraction -- the reference applies attraction instead of repulsion to
+// these pairs (algorithms.cpp:758-768).
+__device__ __noinline__ void correct_neighbours(const MinibatchArgs &a, Cursor c, int ga, int gb,
+                                                const float2 *slice, float2 pi, int sbase, float &fx, float &fy) {
+  // bounded by the target's neighbours inside the slice
+  for (int q = c.next; q < gb; q = c.next) {
+    if (q >= ga) {
+      const float2 pj = slice[q];
+      const float dx = pj.x - pi.x, dy = pj.y - pi.y;
+      const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
+      const float r = rcp_approx(d2);
+      fx = fmaf(dx, r, fx);
+      fy = fmaf(dy, r, fy);
+      attract_pair(a.model, (float)a.W, pj.x, pj.y, pi.x, pi.y, fx, fy);
+    }
+    c.ptr++;
+    c.next = cursor_at(a, c, sbase);
   }
 }
 
@@ -176,7 +243,14 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
   float2 *slice = reinterpret_cast<float2 *>(smem_raw);
   const int slen_pad = (slen + 3) & ~3;
   float2 *gsum = slice + slen_pad;              // [kGroups-1][kChunk]
-  float2 *tpos = gsum + (kGroups - 1) * kChunk;  // [batch]
+  float2 *tbuf = gsum + (kGroups - 1) * kChunk;  // [2][batch]: targets of this and the next batch
+  int *nbmem = reinterpret_cast<int *>(tbuf + 2 * a.batch);  // [2][kChunk * (kNbCap + 2)]
+  auto nblist = [&](unsigned int b) {
+    NbList L;
+    L.ids = nbmem + b * (kChunk * (kNbCap + 2));
+    L.meta = L.ids + kChunk * kNbCap;
+    return L;
+  };
   __shared__ double red[kWarps];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -194,6 +268,8 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
   double e_prev = DBL_MAX, e_cur = 0.0;
   long long loop = 0;
   bool ok = true;
+  bool prefetched = false;
+  unsigned int seq = 0;  // batches processed in this launch
 
   while (ok) {
     if (a.converged) {
@@ -202,11 +278,20 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
       break;
     }
     const bool need_energy = a.converged || (loop == a.iterations - 1);
-    for (int c = 0; c < a.nbatches && ok; c++) {
+    for (int c = 0; c < a.nbatches && ok; c++, seq++) {
       const int base = c * a.batch;
       const int cnt = min(a.batch, a.n - base);
-      const int buf = c & 1;
-      for (int t = tid; t < cnt; t += kThreads) tpos[t] = a.pos[base + t];
+      // buffers alternate by the batch's position in the whole run, so the
+      // last batch of an iteration and the first of the next never share one
+      const int buf = (int)(seq & 1u);
+      float2 *tpos = tbuf + buf * a.batch;
+      // the targets of batch c are normally prefetched during batch c-1;
+      // the first batch of the run, and every batch when there is only one,
+      // loads them here
+      if (!prefetched) {
+        for (int t = tid; t < cnt; t += kThreads) tpos[t] = a.pos[base + t];
+        if (cnt <= kChunk) stage_neighbours(a, nblist(buf), s, base, cnt, slo, shi, sbase);
+      }
       __syncthreads();
       // ---- sweep: partial force of this block's slice on every target ----
       // repulsion for every source, attraction instead for the target's
@@ -217,39 +302,44 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
         const bool v0 = t0 < cnt, v1 = t1 < cnt;
         const float2 p0 = v0 ? tpos[t0] : make_float2(0.f, 0.f);
         const float2 p1 = v1 ? tpos[t1] : make_float2(0.f, 0.f);
+        NbList L = nblist(buf);
+        if (cnt > kChunk) {  // several chunks: stage this chunk's neighbours now
+          __syncthreads();
+          stage_neighbours(a, L, s, base + c0, min(kChunk, cnt - c0), slo, shi, sbase);
+          __syncthreads();
+        }
         Cursor c0r, c1r;
         c0r.next = c1r.next = INT_MAX;
-        if (v0) cursor_init(c0r, a, s, base + t0, slo, sbase + ga, sbase);
-        if (v1) cursor_init(c1r, a, s, base + t1, slo, sbase + ga, sbase);
+        c0r.ptr = c0r.cnt = c1r.ptr = c1r.cnt = 0;
+        if (v0) cursor_init(c0r, a, L, gl, ga, sbase);
+        if (v1) cursor_init(c1r, a, L, gl + kGroup, ga, sbase);
         float fx0a = 0.f, fy0a = 0.f, fx0b = 0.f, fy0b = 0.f;
         float fx1a = 0.f, fy1a = 0.f, fx1b = 0.f, fy1b = 0.f;
+        // branch-free repulsion over the group's sources ...
         int k = ga;
         if ((k & 1) && k < gb) {
           const float2 q = slice[k];
-          pair_exact(a, c0r, k, q.x, q.y, p0.x, p0.y, sbase, fx0a, fy0a);
-          pair_exact(a, c1r, k, q.x, q.y, p1.x, p1.y, sbase, fx1a, fy1a);
+          rep_pair(q.x, q.y, p0.x, p0.y, fx0a, fy0a);
+          rep_pair(q.x, q.y, p1.x, p1.y, fx1a, fy1a);
           k++;
         }
 #pragma unroll 4
         for (; k + 1 < gb; k += 2) {
           const float4 q = *reinterpret_cast<const float4 *>(&slice[k]);
-          if (c0r.next > k + 1 && c1r.next > k + 1) {
-            rep_pair(q.x, q.y, p0.x, p0.y, fx0a, fy0a);
-            rep_pair(q.z, q.w, p0.x, p0.y, fx0b, fy0b);
-            rep_pair(q.x, q.y, p1.x, p1.y, fx1a, fy1a);
-            rep_pair(q.z, q.w, p1.x, p1.y, fx1b, fy1b);
-          } else {
-            pair_exact(a, c0r, k, q.x, q.y, p0.x, p0.y, sbase, fx0a, fy0a);
-            pair_exact(a, c0r, k + 1, q.z, q.w, p0.x, p0.y, sbase, fx0b, fy0b);
-            pair_exact(a, c1r, k, q.x, q.y, p1.x, p1.y, sbase, fx1a, fy1a);
-            pair_exact(a, c1r, k + 1, q.z, q.w, p1.x, p1.y, sbase, fx1b, fy1b);
-          }
+          rep_pair(q.x, q.y, p0.x, p0.y, fx0a, fy0a);
+          rep_pair(q.z, q.w, p0.x, p0.y, fx0b, fy0b);
+          rep_pair(q.x, q.y, p1.x, p1.y, fx1a, fy1a);
+          rep_pair(q.z, q.w, p1.x, p1.y, fx1b, fy1b);
         }
         if (k < gb) {
           const float2 q = slice[k];
-          pair_exact(a, c0r, k, q.x, q.y, p0.x, p0.y, sbase, fx0b, fy0b);
-          pair_exact(a, c1r, k, q.x, q.y, p1.x, p1.y, sbase, fx1b, fy1b);
+          rep_pair(q.x, q.y, p0.x, p0.y, fx0b, fy0b);
+          rep_pair(q.x, q.y, p1.x, p1.y, fx1b, fy1b);
         }
+        // ... then the matched neighbours in [ga, gb): take their repulsion
+        // back (same FP32 formula) and add the model's attraction instead
+        if (v0) correct_neighbours(a, c0r, ga, gb, slice, p0, sbase, fx0b, fy0b);
+        if (v1) correct_neighbours(a, c1r, ga, gb, slice, p1, sbase, fx1b, fy1b);
         const float2 r0 = make_float2(fx0a + fx0b, fy0a + fy0b);
         const float2 r1 = make_float2(fx1a + fx1b, fy1a + fy1b);
         if (grp > 0) {
@@ -265,59 +355,61 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
             o0.x += u0.x; o0.y += u0.y;
             o1.x += u1.x; o1.y += u1.y;
           }
-          float2 *P = a.partials + (size_t)buf * a.batch * a.grid;
-          if (t0 < cnt) P[(size_t)t0 * a.grid + s] = o0;
-          if (t1 < cnt) P[(size_t)t1 * a.grid + s] = o1;
+          long long *A = a.acc + (size_t)buf * a.batch * 2;
+          if (t0 < cnt) {
+            acc_add(&A[2 * t0], o0.x, a.st);
+            acc_add(&A[2 * t0 + 1], o0.y, a.st);
+          }
+          if (t1 < cnt) {
+            acc_add(&A[2 * t1], o1.x, a.st);
+            acc_add(&A[2 * t1 + 1], o1.y, a.st);
+          }
         }
         __syncthreads();
       }
+      // prefetch the next batch's targets and cursors: its vertices do not
+      // move before it, and the cursors depend on the graph only
+      {
+        const int cn = (c + 1 < a.nbatches) ? c + 1 : 0;
+        prefetched = (cn != c);  // a single batch moves itself: reload after the update
+        if (prefetched) {
+          const int nbase = cn * a.batch;
+          const int ncnt = min(a.batch, a.n - nbase);
+          float2 *ntpos = tbuf + (int)((seq + 1u) & 1u) * a.batch;
+          for (int t = tid; t < ncnt; t += kThreads) ntpos[t] = a.pos[nbase + t];
+          if (ncnt <= kChunk) stage_neighbours(a, nblist((seq + 1u) & 1u), s, nbase, ncnt, slo, shi, sbase);
+        }
+      }
       ok = grid_barrier(a.st, epoch);
       if (!ok) break;
-      // ---- owners: sum the partials (float-float, fixed order), update -------
+      // ---- owners: read the summed force, update, clear the accumulator -----
       const int olo = max(slo, base), ohi = min(shi, base + cnt);
       if (olo < ohi) {
-        const float2 *P = a.partials + (size_t)buf * a.batch * a.grid;
+        long long *A = a.acc + (size_t)buf * a.batch * 2;
         const float stepf = (float)step;
-        for (int i = olo + warp; i < ohi; i += kWarps) {
+        for (int i = olo + tid; i < ohi; i += kThreads) {
           const int t = i - base;
-          float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f;
-          for (int q = lane; q < a.grid; q += 32) {
-            const float2 v = __ldcg(&P[(size_t)t * a.grid + q]);
-            ff_add(hx, lx, v.x);
-            ff_add(hy, ly, v.y);
+          const longlong2 v = __ldcg(reinterpret_cast<const longlong2 *>(&A[2 * t]));
+          // cleared for the batch after next, which reuses this buffer
+          *reinterpret_cast<longlong2 *>(&A[2 * t]) = make_longlong2(0, 0);
+          const double dfx = (double)v.x * kFixInv, dfy = (double)v.y * kFixInv;
+          const float2 pi = tpos[t];
+          const float fx = (float)dfx, fy = (float)dfy;
+          float2 np = pi;
+          const float m2 = fmaf(fx, fx, fy * fy);
+          if (m2 >= 1.17549435e-38f && m2 <= 3.0e38f) {
+            const float rm = rsqrt_approx(m2);
+            np.x = fmaf(stepf, fx * rm, pi.x);
+            np.y = fmaf(stepf, fy * rm, pi.y);
+          } else if (fx != 0.f || fy != 0.f) {  // |f|^2 outside the FP32 range
+            const double mag = sqrt(dfx * dfx + dfy * dfy);
+            np.x = (float)((double)pi.x + (dfx / mag) * step);
+            np.y = (float)((double)pi.y + (dfy / mag) * step);
           }
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) {
-            const float ohx = __shfl_xor_sync(0xffffffffu, hx, o);
-            const float olx = __shfl_xor_sync(0xffffffffu, lx, o);
-            const float ohy = __shfl_xor_sync(0xffffffffu, hy, o);
-            const float oly = __shfl_xor_sync(0xffffffffu, ly, o);
-            ff_add(hx, lx, ohx);
-            lx += olx;
-            ff_add(hy, ly, ohy);
-            ly += oly;
-          }
-          if (lane == 0) {
-            const float2 pi = tpos[t];
-            const float fx = hx + lx, fy = hy + ly;
-            float2 np = pi;
-            const float m2 = fmaf(fx, fx, fy * fy);
-            if (m2 >= 1.17549435e-38f && m2 <= 3.0e38f) {
-              const float rm = rsqrt_approx(m2);
-              np.x = fmaf(stepf, fx * rm, pi.x);
-              np.y = fmaf(stepf, fy * rm, pi.y);
-            } else if (fx != 0.f || fy != 0.f) {  // |f|^2 outside the FP32 range
-              const double dfx = (double)hx + (double)lx, dfy = (double)hy + (double)ly;
-              const double mag = sqrt(dfx * dfx + dfy * dfy);
-              np.x = (float)((double)pi.x + (dfx / mag) * step);
-              np.y = (float)((double)pi.y + (dfy / mag) * step);
-            }
-            a.pos[i] = np;
-            slice[i - sbase] = np;
-            const double dfx = (double)hx + (double)lx, dfy = (double)hy + (double)ly;
-            a.force[i] = make_double2(dfx, dfy);
-            a.e[i] = dfx * dfx + dfy * dfy;
-          }
+          a.pos[i] = np;
+          slice[i - sbase] = np;
+          a.force[i] = make_double2(dfx, dfy);
+          a.e[i] = dfx * dfx + dfy * dfy;
         }
       }
       // owner warps still read tpos and write the slice: finish before the
@@ -372,7 +464,8 @@ __global__ void cursor_table_kernel(const int *__restrict__ rowptr, const int *_
 }  // namespace
 
 int ensure_minibatch_scratch(bl_ctx *ctx, int batch, int grid) {
-  const size_t need = (size_t)2 * batch * grid * sizeof(float2);
+  (void)grid;
+  const size_t need = (size_t)2 * batch * 2 * sizeof(long long);
   if (ctx->s.partials_bytes < need) {
     if (ctx->s.partials) cudaFree(ctx->s.partials);
     ctx->s.partials = nullptr;
@@ -402,7 +495,8 @@ int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step
   cudaDeviceGetAttribute(&dev_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
   auto smem_for = [&](int g) {
     const int slice_max = (n + g - 1) / g + 2;
-    return (size_t)(((slice_max + 3) & ~3) + (kGroups - 1) * kChunk + batch) * sizeof(float2);
+    return (size_t)(((slice_max + 3) & ~3) + (kGroups - 1) * kChunk + 2 * batch) * sizeof(float2) +
+           (size_t)2 * kChunk * (kNbCap + 2) * sizeof(int);
   };
   while (smem_for(grid) + 1024 > (size_t)dev_smem_optin && grid < ctx->num_sms) grid++;
   const size_t smem = smem_for(grid);
@@ -428,6 +522,7 @@ int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step
     ctx->s.cursor_grid = grid;
   }
   BL_CUDA(ctx, cudaMemsetAsync(ctx->s.status, 0, sizeof(DevStatus), ctx->stream));
+  BL_CUDA(ctx, cudaMemsetAsync(ctx->s.partials, 0, (size_t)2 * batch * 2 * sizeof(long long), ctx->stream));
 
   MinibatchArgs a;
   a.n = n;
@@ -442,7 +537,7 @@ int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step
   a.pos = ctx->pos;
   a.force = ctx->force;
   a.e = ctx->e;
-  a.partials = ctx->s.partials;
+  a.acc = reinterpret_cast<long long *>(ctx->s.partials);
   a.energy = ctx->s.energy;
   a.energy_parts = ctx->s.energy_parts;
   a.loops = reinterpret_cast<long long *>(ctx->s.energy + 1);
@@ -484,8 +579,8 @@ int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step
 // in the fixed array below, so the call allocates nothing.  The caller passes
 // its inputs and outputs as device pointers.
 //
-// Limits: batch <= 256 and at most 160 blocks (one per SM), so the scratch is
-// at most 2 * 256 * 160 float2 partials plus a few hundred bytes: 768 KiB.
+// Limits: batch <= 256 and at most 160 blocks (one per SM); the scratch is a
+// fixed 768 KiB (force accumulators, energy partials, status word).
 // The array exists once per device for the lifetime of the process and every
 // call on that device shares it: calls that overlap on the GPU (different
 // streams, or host threads that do not serialise) race and give wrong
@@ -543,7 +638,8 @@ extern "C" int bl_minibatch_iteration_noalloc(int n, const int *d_rowptr, const 
   int grid = std::min(num_sms, std::max(1, (n + 127) / 128));
   auto smem_for = [&](int g) {
     const int slice_max = (n + g - 1) / g + 2;
-    return (size_t)(((slice_max + 3) & ~3) + (kGroups - 1) * kChunk + batch) * sizeof(float2);
+    return (size_t)(((slice_max + 3) & ~3) + (kGroups - 1) * kChunk + 2 * batch) * sizeof(float2) +
+           (size_t)2 * kChunk * (kNbCap + 2) * sizeof(int);
   };
   while (smem_for(grid) + 1024 > (size_t)smem_optin && grid < num_sms) grid++;
   if (grid > kNoAllocMaxGrid) return BL_ERR_TOO_LARGE;  // scratch holds 160 blocks of partials
@@ -556,15 +652,17 @@ extern "C" int bl_minibatch_iteration_noalloc(int n, const int *d_rowptr, const 
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, minibatch_kernel, kThreads, smem) != cudaSuccess ||
       occ < 1 || grid > occ * num_sms)
     return BL_ERR_TOO_LARGE;
-  // carve the scratch: partials | energy parts | energy + loops | status
+  // carve the scratch: force accumulators | energy parts | energy + loops | status
   float2 *partials = reinterpret_cast<float2 *>(base);
   double *energy_parts = reinterpret_cast<double *>(base + kNoAllocPartialBytes);
   double *energy = energy_parts + kNoAllocMaxGrid;
   DevStatus *status = reinterpret_cast<DevStatus *>(energy + 4);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // the status word (barrier counter, error code) must start at zero; every
-  // other scratch value is written before it is read
+  // the status word (barrier counter, error code) and the force accumulators
+  // must start at zero; every other scratch value is written before it is read
   if (cudaMemsetAsync(status, 0, sizeof(DevStatus), st) != cudaSuccess) return BL_ERR_CUDA;
+  if (cudaMemsetAsync(partials, 0, (size_t)2 * batch * 2 * sizeof(long long), st) != cudaSuccess)
+    return BL_ERR_CUDA;
   MinibatchArgs a;
   a.n = n;
   a.batch = batch;
@@ -578,7 +676,7 @@ extern "C" int bl_minibatch_iteration_noalloc(int n, const int *d_rowptr, const 
   a.pos = reinterpret_cast<float2 *>(d_xy);
   a.force = reinterpret_cast<double2 *>(d_force);
   a.e = d_vertex_energy;
-  a.partials = partials;
+  a.acc = reinterpret_cast<long long *>(partials);
   a.energy = energy;
   a.energy_parts = energy_parts;
   a.loops = reinterpret_cast<long long *>(energy + 1);

@@ -333,3 +333,22 @@ def test_chunglu100k_minibatch_iteration_forces(B):
     tf, te = oracle.forces_on_trajectory(2, g.rowptr, g.colids, xy, xe, 256)
     assert rel_l2(f, tf) <= FORCE_TOL
     assert abs(e - te) / te <= 2 * FORCE_TOL
+
+
+@pytest.mark.parametrize("model", [2, 3])
+def test_multi_iteration_launch_equals_single_iterations(B, model):
+    """One launch running 3 iterations (buffers alternating across the
+    iteration boundary with an odd batch count: 410 vertices / 32 = 13
+    batches) gives bit-identical coordinates to 3 one-iteration launches."""
+    z = load_golden("rgg")
+    decay = 0.999 if model == 2 else 0.99
+    with make(B, z) as a:
+        a.run_resident(model, 3, 32, 1.2, 1.0)
+        multi = a.nCoordinates
+    with make(B, z) as a:
+        step = 1.0
+        for _ in range(3):
+            a.minibatch_iteration(model, 32, step)
+            step *= decay
+        single = a.nCoordinates
+    assert np.array_equal(multi, single)
