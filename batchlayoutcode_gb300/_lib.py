@@ -23,7 +23,8 @@ EXPORTS = (
     "bl_write_to_file", "bl_minibatch_iteration", "bl_barnes_hut_iteration", "bl_morton_order",
     "bl_quadtree", "bl_bh_repulsion", "bl_run_resident", "bl_set_graph_mode", "bl_last_kernel_time",
     "bl_kernel_launches", "bl_last_run_ms", "bl_random_coordinates", "bl_greedy_coordinates", "bl_write_coordinates",
-    "bl_minibatch_iteration_noalloc",
+    "bl_minibatch_iteration_noalloc", "bl_batch_create", "bl_batched_prepare", "bl_batched_run",
+    "bl_batched_result", "bl_batched_layout", "bl_batched_parts", "bl_batched_set_parts",
 )
 
 _lib = None
@@ -81,6 +82,14 @@ def load() -> C.CDLL:
         "bl_greedy_coordinates": (i32, [i32, ip, ip, dp]),
         "bl_write_coordinates": (i32, [cp, cp, cp, dp, i32, cp, i32]),
         "bl_minibatch_iteration_noalloc": (i32, [i32, vp, vp, vp, vp, vp, i32, i32, f64, f64, dp, vp]),
+        "bl_batch_create": (vp, [i32]),
+        "bl_batched_prepare": (i32, [vp, i32, ip, C.POINTER(C.c_longlong), ip, ip, ip, dp]),
+        "bl_batched_run": (i32, [vp, i32, i32, f64, f64, dp]),
+        "bl_batched_result": (i32, [vp, dp, dp]),
+        "bl_batched_layout": (i32, [vp, i32, ip, C.POINTER(C.c_longlong), ip, ip, ip, dp, i32, i32, f64, f64, dp,
+                                    dp]),
+        "bl_batched_parts": (i32, [vp, ip]),
+        "bl_batched_set_parts": (i32, [vp, ip]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -319,3 +328,83 @@ class Algorithms:
 
     def kernel_launches(self) -> int:
         return int(self._L.bl_kernel_launches(self._ctx))
+
+
+class BatchedLayout:
+    """Many independent graphs laid out by one persistent launch (no
+    counterpart in the reference, which runs one graph per process).
+
+    graphs: sequence of (rowptr, colids) CSR pairs with local vertex ids;
+    algo: per-graph algorithm (2, 3, 8 minibatch or 4 Barnes-Hut), or one int
+    for all; xy: per-graph (n, 2) starting coordinates."""
+
+    def __init__(self, graphs, algo, xy, device: int = 0):
+        L = load()
+        self._L = L
+        ctx = L.bl_batch_create(device)
+        if not ctx:
+            raise BatchLayoutError(-2, "bl_batch_create failed")
+        self._ctx = ctx
+        G = len(graphs)
+        sizes = np.array([len(rp) - 1 for rp, _ in graphs], np.int64)
+        self.vertex_offset = np.zeros(G + 1, np.int32)
+        self.vertex_offset[1:] = np.cumsum(sizes)
+        self.edge_offset = np.zeros(G + 1, np.int64)
+        self.edge_offset[1:] = np.cumsum([len(ci) for _, ci in graphs])
+        self.rowptr = np.ascontiguousarray(np.concatenate([np.asarray(rp, np.int32) for rp, _ in graphs]))
+        self.colids = np.ascontiguousarray(
+            np.concatenate([np.asarray(ci, np.int32) for _, ci in graphs] + [np.zeros(1, np.int32)]))
+        self.algo = np.ascontiguousarray(np.broadcast_to(np.asarray(algo, np.int32), (G,)).copy())
+        self.xy0 = np.ascontiguousarray(np.concatenate([np.asarray(x, np.float64).reshape(-1, 2) for x in xy]))
+        self.sizes = sizes
+        self._check(L.bl_batched_prepare(ctx, G, _ip(self.vertex_offset),
+                                         self.edge_offset.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                         _ip(self.rowptr), _ip(self.colids), _ip(self.algo), _dp(self.xy0)))
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise BatchLayoutError(rc, self._L.bl_last_error(self._ctx).decode())
+
+    def run(self, iterations: int, batch: int = 256, theta: float = 1.2, weight: float = 1.0) -> float:
+        """Lay out every graph; returns the device seconds of the run."""
+        secs = C.c_double()
+        self._check(self._L.bl_batched_run(self._ctx, iterations, batch, theta, weight, C.byref(secs)))
+        return secs.value
+
+    def result(self):
+        """-> (list of per-graph (n, 2) coordinates, per-graph energies)."""
+        xy = np.zeros((int(self.vertex_offset[-1]), 2))
+        e = np.zeros(len(self.sizes))
+        self._check(self._L.bl_batched_result(self._ctx, _dp(xy), _dp(e)))
+        vo = self.vertex_offset
+        return [xy[vo[g]:vo[g + 1]] for g in range(len(self.sizes))], e
+
+    def parts(self):
+        """Source ranges per target chosen for minibatch graphs (< 512, < 2048, >= 2048 vertices)."""
+        out = np.zeros(3, np.int32)
+        self._check(self._L.bl_batched_parts(self._ctx, _ip(out)))
+        return out
+
+    def set_parts(self, parts3):
+        a = np.ascontiguousarray(parts3, np.int32)
+        self._check(self._L.bl_batched_set_parts(self._ctx, _ip(a)))
+
+    def kernel_launches(self) -> int:
+        return int(self._L.bl_kernel_launches(self._ctx))
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._L.bl_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

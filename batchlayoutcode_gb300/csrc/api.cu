@@ -74,6 +74,34 @@ static void collect_timing(bl_ctx *ctx) {
   ctx->ev_used = 0;
 }
 
+// Neighbours the sorted-CSR cursor of the minibatch sweep matches
+// (sample/algorithms.cpp:746, 758-762): the cursor starts at rowptr[i] and
+// advances after a match while it is below rowptr[i+1]-1, as the source index
+// j increases.  It matches the strictly increasing prefix of the row; for an
+// empty row it reads colids[rowptr[i]], the first entry of a later row.
+void bl::cursor_neighbours(int n, const std::vector<int> &rp, const std::vector<int> &ci,
+                       std::vector<int> &erp, std::vector<int> &eci) {
+  const long long nnz = rp[n];
+  erp.assign(n + 1, 0);
+  eci.clear();
+  eci.reserve(ci.size());
+  for (int i = 0; i < n; i++) {
+    const int k0 = rp[i], k1 = rp[i + 1];
+    if (k1 > k0) {
+      int last = ci[k0];
+      eci.push_back(last);
+      for (int k = k0 + 1; k < k1; k++) {
+        if (ci[k] <= last) break;
+        last = ci[k];
+        eci.push_back(last);
+      }
+    } else if (k0 < nnz) {
+      eci.push_back(ci[k0]);
+    }
+    erp[i + 1] = (int)eci.size();
+  }
+}
+
 namespace {
 
 double wall() {
@@ -109,38 +137,12 @@ void free_ctx(bl_ctx *c) {
     fr(ls.early_off);
     fr(ls.early_col);
   }
+  bl::batched_free(c->batched);
+  c->batched = nullptr;
   for (auto ev : c->ev_pool) cudaEventDestroy(ev);
   for (auto ev : c->run_ev)
     if (ev) cudaEventDestroy(ev);
   if (c->stream) cudaStreamDestroy(c->stream);
-}
-
-// Neighbours the sorted-CSR cursor of the minibatch sweep matches
-// (sample/algorithms.cpp:746, 758-762): the cursor starts at rowptr[i] and
-// advances after a match while it is below rowptr[i+1]-1, as the source index
-// j increases.  It matches the strictly increasing prefix of the row; for an
-// empty row it reads colids[rowptr[i]], the first entry of a later row.
-void cursor_neighbours(int n, const std::vector<int> &rp, const std::vector<int> &ci,
-                       std::vector<int> &erp, std::vector<int> &eci) {
-  const long long nnz = rp[n];
-  erp.assign(n + 1, 0);
-  eci.clear();
-  eci.reserve(ci.size());
-  for (int i = 0; i < n; i++) {
-    const int k0 = rp[i], k1 = rp[i + 1];
-    if (k1 > k0) {
-      int last = ci[k0];
-      eci.push_back(last);
-      for (int k = k0 + 1; k < k1; k++) {
-        if (ci[k] <= last) break;
-        last = ci[k];
-        eci.push_back(last);
-      }
-    } else if (k0 < nnz) {
-      eci.push_back(ci[k0]);
-    }
-    erp[i + 1] = (int)eci.size();
-  }
 }
 
 int init_coordinates(bl_ctx *ctx) {
@@ -234,7 +236,7 @@ bl_ctx *bl_algorithms_create(int device, int n, long long nnz, const int *rowptr
   ctx->h_rowptr.assign(rowptr, rowptr + n + 1);
   ctx->h_colids.assign(colids, colids + nnz);
   std::vector<int> erp, eci;
-  cursor_neighbours(n, ctx->h_rowptr, ctx->h_colids, erp, eci);
+  bl::cursor_neighbours(n, ctx->h_rowptr, ctx->h_colids, erp, eci);
   const size_t cn = std::max<long long>(nnz, 1);
   if ((e = cudaMalloc(&ctx->g.rowptr, (n + 1) * sizeof(int))) != cudaSuccess) return bad(e, "cudaMalloc");
   if ((e = cudaMalloc(&ctx->g.colids, cn * sizeof(int))) != cudaSuccess) return bad(e, "cudaMalloc");

@@ -33,20 +33,11 @@
 #include <cmath>
 #include <cstring>
 
-#include "bl_internal.cuh"
+#include "bh_device.cuh"
 
 namespace bl {
 namespace {
 
-typedef unsigned long long u64;
-
-__device__ __forceinline__ unsigned int f2ord(float f) {
-  const unsigned int u = __float_as_uint(f);
-  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-__device__ __forceinline__ float ord2f(unsigned int u) {
-  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
-}
 
 __global__ void bbox_init_kernel(unsigned int *bbox) {
   if (threadIdx.x == 0) {
@@ -79,41 +70,6 @@ __global__ void bbox_kernel(const float2 *__restrict__ pos, int n, unsigned int 
   }
 }
 
-__device__ __forceinline__ u64 spread32(unsigned int v) {
-  u64 x = v;
-  x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
-  x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
-  x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
-  x = (x | (x << 2)) & 0x3333333333333333ull;
-  x = (x | (x << 1)) & 0x5555555555555555ull;
-  return x;
-}
-
-// Frame (MortonCode.h:42-52) from the bbox; FP64 like the reference.
-__device__ __forceinline__ void frame_from_bbox(const unsigned int *bbox, double &minX,
-                                                double &minY, double &maxmin) {
-  minX = (double)ord2f(bbox[0]);
-  const double maxX = (double)ord2f(bbox[1]);
-  minY = (double)ord2f(bbox[2]);
-  const double maxY = (double)ord2f(bbox[3]);
-  const double ry = __dsub_rn(maxY, minY), rx = __dsub_rn(maxX, minX);
-  maxmin = (ry < rx) ? rx : ry;  // std::max(y-range, x-range)
-}
-
-// (uint32)(4294967295.0 * (v - mn) / maxmin), MortonCode.h:62-67, no contraction.
-// The quotient is formed with the reciprocal (one multiply); its error is a
-// few ulp, so unless it lies within 4 ulp of an integer its truncation equals
-// the truncation of the correctly rounded quotient.  Otherwise the exact
-// division decides.
-__device__ __forceinline__ unsigned int quantise(float v, double mn, double maxmin, double inv) {
-  if (!(maxmin > 0.0)) return 0u;
-  const double a = __dmul_rn(4294967295.0, __dsub_rn((double)v, mn));
-  const double qf = __dmul_rn(a, inv);
-  const double fl = floor(qf);
-  const double eps = 4.0 * fabs(qf) * 1.1102230246251565e-16 + 1e-300;
-  if (qf - fl > eps && (fl + 1.0) - qf > eps) return __double2uint_rz(fl);
-  return __double2uint_rz(__ddiv_rn(a, maxmin));
-}
 
 __global__ void frame_kernel(const unsigned int *bbox, double *frame) {
   if (threadIdx.x != 0) return;
@@ -130,9 +86,7 @@ __global__ void morton_kernel(const float2 *__restrict__ pos, int n, u64 *keys, 
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double minX = frame[0], minY = frame[1], maxmin = frame[2], inv = frame[3];
-  const float2 p = pos[i];
-  keys[i] = (spread32(quantise(p.y, minY, maxmin, inv)) << 1) |
-            spread32(quantise(p.x, minX, maxmin, inv));
+  keys[i] = morton_key(pos[i], minX, minY, maxmin, inv);
   vals[i] = i;
 }
 
@@ -341,23 +295,6 @@ struct TreeArgs {
 constexpr int kNoChild = INT_MIN;
 constexpr int kLevels = 33;  // digit levels 0..31 plus 32 for runs of equal keys
 
-// x / c for the child count c of a quad node, correctly rounded like the
-// reference's `c_x /= count` (BarnesHut.h:214-216) but without a division:
-// c = 2 and 4 scale exactly; for c = 3 the product with RN(1/3) is corrected
-// once with its exact FMA residual (Markstein, "IA-64 and Elementary
-// Functions", 2000), which is correctly rounded because x/3 is never a tie.
-__device__ __forceinline__ double div_count(double x, int c) {
-  if (c == 1) return x;
-  if (c == 2) return __dmul_rn(x, 0.5);
-  if (c == 4) return __dmul_rn(x, 0.25);
-  if (c == 3) {
-    const double r3 = 0.33333333333333331;  // RN(1/3)
-    const double q0 = __dmul_rn(x, r3);
-    const double r = __fma_rn(-3.0, q0, x);
-    return __fma_rn(r, r3, q0);
-  }
-  return __ddiv_rn(x, (double)c);
-}
 
 // Internal node merged into its parent's quad node: the x-bit split of the
 // digit whose y-bit split is the parent, or any split inside a run of equal
@@ -581,104 +518,26 @@ struct TraverseArgs {
   float W;
 };
 
-// Compensated float-float accumulation (Knuth's TwoSum): hi + lo carries the
-// sum of FP32 terms to about 48 bits without touching the FP64 pipe.
-__device__ __forceinline__ void ff_add(float &hi, float &lo, float t) {
-  const float s = hi + t;
-  const float bb = s - hi;
-  const float err = (hi - (s - bb)) + (t - bb);
-  hi = s;
-  lo += err;
-}
-
-// FP64 opening test exactly as BarnesHut.h:71-72: diameter / distance < theta.
-__device__ __noinline__ bool open_test_fp64(const double2 *__restrict__ c64,
-                                            const unsigned char *__restrict__ lvl,
-                                            const double *__restrict__ frame, double theta,
-                                            int idx, float qx, float qy) {
-  const double2 c = c64[idx];
-  const double D = ldexp(frame[2], -(int)lvl[idx]);
-  const double dx = __dsub_rn(c.x, (double)qx), dy = __dsub_rn(c.y, (double)qy);
-  const double dist = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
-  return __ddiv_rn(D, dist) < theta;
-}
 
 __global__ void __launch_bounds__(256) traverse_kernel(TraverseArgs a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= a.n) return;
   if (ld_volatile_u32(&a.st->code) != 0u) return;  // the tree of this iteration is not valid
   const float2 q = a.spos[k];
-  const float qm = fabsf(q.x) + fabsf(q.y);
   // record 0 is the root; its skip link is the number of records
   int total = __float_as_int(__ldg(&a.nodes[0]).w);
   if (total < 0 || total > 2 * a.n - 1) {
     dev_record_error(a.st, DEV_BAD_INDEX);
     total = 0;
   }
-  float fx = 0.f, fy = 0.f;
   unsigned int visits = 0, exact = 0;
-  int i = 0;
-  while (i < total) {
-    const float4 nd = __ldg(&a.nodes[i]);
-    const float dx = nd.x - q.x, dy = nd.y - q.y;
-    const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
-    const float lhs = a.theta2 * d2;
-    bool accept = nd.z < lhs;
-    if (nd.z > 0.f) {
-      // error bound of the FP32 comparison (centroid rounding, subtraction,
-      // squares, theta^2 and D^2 rounding), with a wide safety factor
-      const float tol = 9.5367432e-07f * (lhs + nd.z) +
-                        a.theta2 * 4.7683716e-07f * (fabsf(dx) + fabsf(dy)) *
-                            (qm + fabsf(nd.x) + fabsf(nd.y));
-      if (fabsf(lhs - nd.z) <= tol) {
-        accept = open_test_fp64(a.nodes_c64, a.nodes_lvl, a.frame, a.theta, i, q.x, q.y);
-        exact++;
-      }
-    }
-    visits++;
-    if (accept) {
-      const float r = rsqrt_approx(d2);
-      fx = fmaf(dx, r, fx);
-      fy = fmaf(dy, r, fy);
-      const int nxt = __float_as_int(nd.w);
-      if (nxt <= i) {  // a skip link always moves forward; stop on a corrupt one
-        dev_record_error(a.st, DEV_BAD_INDEX);
-        break;
-      }
-      i = nxt;
-    } else {
-      i++;
-    }
-  }
+  const float2 rep = bh_repulsion<true>(a.nodes, a.nodes_c64, a.nodes_lvl, a.frame[2], a.theta2, a.theta, total, q, a.st,
+                                  visits, exact);
   const int v = a.perm[k];
-  a.rep[v] = make_float2(fx, fy);
-  if (a.f0) {
-    // FR attraction (algorithms.cpp:1056-1058) over the neighbours j that are
-    // not moved before v in this iteration (j at or after v's batch start)
-    const float2 pv = a.pold[v];
-    const int batch_lo = (v / a.batch) * a.batch;
-    float hx = -fx, lx = 0.f, hy = -fy, ly = 0.f;
-    const int e1 = a.rowptr[v + 1];
-    constexpr int kU = 4;  // index loads first, then position loads, then the ordered sum
-    for (int e = a.rowptr[v]; e < e1; e += kU) {
-      int j[kU];
-      float2 pj[kU];
-#pragma unroll
-      for (int u = 0; u < kU; u++) j[u] = (e + u < e1) ? a.colids[e + u] : -1;
-#pragma unroll
-      for (int u = 0; u < kU; u++)
-        if (j[u] >= batch_lo) pj[u] = a.pold[j[u]];
-#pragma unroll
-      for (int u = 0; u < kU; u++) {
-        if (j[u] < batch_lo) continue;  // moved earlier in this iteration, or past the row end
-        const float dx = pj[u].x - pv.x, dy = pj[u].y - pv.y;
-        const float sc = a.W * sqrtf(fmaf(dx, dx, dy * dy));
-        ff_add(hx, lx, dx * sc);
-        ff_add(hy, ly, dy * sc);
-      }
-    }
-    a.f0[v] = make_float4(hx, hy, lx, ly);
-  }
+  a.rep[v] = rep;
+  // FR attraction (algorithms.cpp:1056-1058) of the neighbours that have not
+  // moved before v in this iteration
+  if (a.f0) a.f0[v] = bh_unmoved_attraction(v, rep, a.rowptr, a.colids, a.pold, a.batch, a.W);
   if (a.stats) {
     atomicAdd(&a.stats[0], (unsigned long long)visits);
     if (exact) atomicAdd(&a.stats[1], (unsigned long long)exact);
@@ -713,26 +572,8 @@ __device__ __forceinline__ void sweep_vertex(const SweepArgs &a, int t) {
   const float4 f = a.f0[i];
   float hx = f.x, hy = f.y, lx = f.z, ly = f.w;
   const int e1 = a.early_off[t + 1];
-  for (int e = a.early_off[t]; e < e1; e++) {
-    const float2 pj = __ldcg(&a.pnew[a.early_col[e]]);
-    const float dx = pj.x - pi.x, dy = pj.y - pi.y;
-    const float sc = a.W * sqrtf(fmaf(dx, dx, dy * dy));
-    ff_add(hx, lx, dx * sc);
-    ff_add(hy, ly, dy * sc);
-  }
-  const float fxf = hx + lx, fyf = hy + ly;
-  float2 np = pi;
-  const float m2 = fmaf(fxf, fxf, fyf * fyf);
-  if (m2 >= 1.17549435e-38f && m2 <= 3.0e38f) {
-    const float rm = rsqrt_approx(m2);
-    np.x = fmaf(a.step, fxf * rm, pi.x);
-    np.y = fmaf(a.step, fyf * rm, pi.y);
-  } else if (fxf != 0.f || fyf != 0.f) {  // |f|^2 outside the FP32 range
-    const double fx = (double)hx + (double)lx, fy = (double)hy + (double)ly;
-    const double mag = sqrt(fx * fx + fy * fy);
-    np.x = (float)((double)pi.x + (fx / mag) * (double)a.step);
-    np.y = (float)((double)pi.y + (fy / mag) * (double)a.step);
-  }
+  for (int e = a.early_off[t]; e < e1; e++) bh_attract(__ldcg(&a.pnew[a.early_col[e]]), pi, a.W, hx, lx, hy, ly);
+  const float2 np = bh_step(pi, hx, lx, hy, ly, a.step);
   a.pnew[i] = np;
   if (a.write_out) {
     const double fx = (double)hx + (double)lx, fy = (double)hy + (double)ly;

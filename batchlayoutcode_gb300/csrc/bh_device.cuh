@@ -1,0 +1,212 @@
+// bh_device.cuh -- Barnes-Hut arithmetic shared by the whole-device pipeline
+// (barnes_hut.cu) and the one-block-per-graph path (batched.cu), so that both
+// produce the same bits for the same graph.
+//
+// Reference: sample/MortonCode.h:42-97 (frame, quantisation, order),
+// sample/BarnesHut.h:69-86 (opening test, unit-vector repulsion),
+// :197-217 (centroids), sample/algorithms.cpp:1050-1066 (attraction, update).
+#pragma once
+
+#include <climits>
+
+#include "bl_device.cuh"
+
+namespace bl {
+
+typedef unsigned long long u64;
+
+// order-preserving map of a float onto uint32 (for integer min/max)
+__device__ __forceinline__ unsigned int f2ord(float f) {
+  const unsigned int u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned int u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__device__ __forceinline__ u64 spread32(unsigned int v) {
+  u64 x = v;
+  x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
+  x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
+  x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
+  x = (x | (x << 2)) & 0x3333333333333333ull;
+  x = (x | (x << 1)) & 0x5555555555555555ull;
+  return x;
+}
+
+// Frame (MortonCode.h:42-52) from the ordered-uint bbox {min x, max x, min y,
+// max y}; FP64 like the reference.
+__device__ __forceinline__ void frame_from_bbox(const unsigned int *bbox, double &minX, double &minY,
+                                                double &maxmin) {
+  minX = (double)ord2f(bbox[0]);
+  const double maxX = (double)ord2f(bbox[1]);
+  minY = (double)ord2f(bbox[2]);
+  const double maxY = (double)ord2f(bbox[3]);
+  const double ry = __dsub_rn(maxY, minY), rx = __dsub_rn(maxX, minX);
+  maxmin = (ry < rx) ? rx : ry;  // std::max(y-range, x-range)
+}
+
+// (uint32)(4294967295.0 * (v - mn) / maxmin), MortonCode.h:62-67, no contraction.
+// The quotient is formed with the reciprocal (one multiply); its error is a
+// few ulp, so unless it lies within 4 ulp of an integer its truncation equals
+// the truncation of the correctly rounded quotient.  Otherwise the exact
+// division decides.
+__device__ __forceinline__ unsigned int quantise(float v, double mn, double maxmin, double inv) {
+  if (!(maxmin > 0.0)) return 0u;
+  const double a = __dmul_rn(4294967295.0, __dsub_rn((double)v, mn));
+  const double qf = __dmul_rn(a, inv);
+  const double fl = floor(qf);
+  const double eps = 4.0 * fabs(qf) * 1.1102230246251565e-16 + 1e-300;
+  if (qf - fl > eps && (fl + 1.0) - qf > eps) return __double2uint_rz(fl);
+  return __double2uint_rz(__ddiv_rn(a, maxmin));
+}
+
+// 64-bit Morton key, y bit above x bit of every digit (MortonCode.h:83-97).
+__device__ __forceinline__ u64 morton_key(float2 p, double minX, double minY, double maxmin, double inv) {
+  return (spread32(quantise(p.y, minY, maxmin, inv)) << 1) | spread32(quantise(p.x, minX, maxmin, inv));
+}
+
+// x / c for the child count c of a quad node, correctly rounded like the
+// reference's `c_x /= count` (BarnesHut.h:214-216) but without a division:
+// c = 2 and 4 scale exactly; for c = 3 the product with RN(1/3) is corrected
+// once with its exact FMA residual (Markstein, "IA-64 and Elementary
+// Functions", 2000), which is correctly rounded because x/3 is never a tie.
+__device__ __forceinline__ double div_count(double x, int c) {
+  if (c == 1) return x;
+  if (c == 2) return __dmul_rn(x, 0.5);
+  if (c == 4) return __dmul_rn(x, 0.25);
+  if (c == 3) {
+    const double r3 = 0.33333333333333331;  // RN(1/3)
+    const double q0 = __dmul_rn(x, r3);
+    const double r = __fma_rn(-3.0, q0, x);
+    return __fma_rn(r, r3, q0);
+  }
+  return __ddiv_rn(x, (double)c);
+}
+
+// Loads of the tree records and positions: through the read-only data cache
+// (kRO) when the launch does not write them, plain loads otherwise (the
+// one-block path rewrites them every iteration, ordered by block barriers).
+template <bool kRO, typename T>
+__device__ __forceinline__ T ldx(const T *p) {
+  if constexpr (kRO) return __ldg(p);
+  else return *p;
+}
+
+// FP64 opening test exactly as BarnesHut.h:71-72: diameter / distance < theta.
+template <bool kRO>
+static __device__ __noinline__ bool open_test_fp64(const double2 *c64, const unsigned char *lvl, double maxmin,
+                                                   double theta, int idx, float qx, float qy) {
+  const double2 c = ldx<kRO>(&c64[idx]);
+  const double D = ldexp(maxmin, -(int)ldx<kRO>(&lvl[idx]));
+  const double dx = __dsub_rn(c.x, (double)qx), dy = __dsub_rn(c.y, (double)qy);
+  const double dist = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+  return __ddiv_rn(D, dist) < theta;
+}
+
+// Stackless walk of the pre-order records {x, y, D^2, skip} (record 0 is the
+// root, its skip link is the number of records): repulsion on q
+// (BarnesHut.h:69-86).  The opening test D/dist < theta is evaluated in FP32
+// and re-evaluated in FP64 when the FP32 margin is within its error bound, so
+// every decision equals the reference's FP64 decision.  A leaf at q itself
+// adds nothing (its vector is zero).
+template <bool kRO>
+__device__ __forceinline__ float2 bh_repulsion(const float4 *nodes, const double2 *c64, const unsigned char *lvl,
+                                               double maxmin, float theta2, double theta, int total, float2 q,
+                                               DevStatus *st, unsigned int &visits, unsigned int &exact) {
+  const float qm = fabsf(q.x) + fabsf(q.y);
+  float fx = 0.f, fy = 0.f;
+  int i = 0;
+  while (i < total) {
+    const float4 nd = ldx<kRO>(&nodes[i]);
+    const float dx = nd.x - q.x, dy = nd.y - q.y;
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
+    const float lhs = theta2 * d2;
+    bool accept = nd.z < lhs;
+    if (nd.z > 0.f) {
+      // error bound of the FP32 comparison (centroid rounding, subtraction,
+      // squares, theta^2 and D^2 rounding), with a wide safety factor
+      const float tol = 9.5367432e-07f * (lhs + nd.z) +
+                        theta2 * 4.7683716e-07f * (fabsf(dx) + fabsf(dy)) * (qm + fabsf(nd.x) + fabsf(nd.y));
+      if (fabsf(lhs - nd.z) <= tol) {
+        accept = open_test_fp64<kRO>(c64, lvl, maxmin, theta, i, q.x, q.y);
+        exact++;
+      }
+    }
+    visits++;
+    if (accept) {
+      const float r = rsqrt_approx(d2);
+      fx = fmaf(dx, r, fx);
+      fy = fmaf(dy, r, fy);
+      const int nxt = __float_as_int(nd.w);
+      if (nxt <= i) {  // a skip link always moves forward; stop on a corrupt one
+        dev_record_error(st, DEV_BAD_INDEX);
+        break;
+      }
+      i = nxt;
+    } else {
+      i++;
+    }
+  }
+  return make_float2(fx, fy);
+}
+
+// FR attraction of one neighbour (algorithms.cpp:1056-1058) added to the
+// float-float sum (hx, lx), (hy, ly).
+__device__ __forceinline__ void bh_attract(float2 pj, float2 pv, float W, float &hx, float &lx, float &hy,
+                                           float &ly) {
+  const float dx = pj.x - pv.x, dy = pj.y - pv.y;
+  const float sc = W * sqrtf(fmaf(dx, dx, dy * dy));
+  ff_add(hx, lx, dx * sc);
+  ff_add(hy, ly, dy * sc);
+}
+
+// Minus the repulsion plus the attraction of the neighbours j of v that are
+// not moved before v in this iteration (j at or after v's batch start), read
+// at their iteration-start positions; CSR order, float-float.
+__device__ __forceinline__ float4 bh_unmoved_attraction(int v, float2 rep, const int *__restrict__ rowptr,
+                                                        const int *__restrict__ colids, const float2 *pold, int batch,
+                                                        float W) {
+  const float2 pv = pold[v];
+  const int batch_lo = (v / batch) * batch;
+  float hx = -rep.x, lx = 0.f, hy = -rep.y, ly = 0.f;
+  const int e1 = rowptr[v + 1];
+  constexpr int kU = 4;  // index loads first, then position loads, then the ordered sum
+  for (int e = rowptr[v]; e < e1; e += kU) {
+    int j[kU];
+    float2 pj[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) j[u] = (e + u < e1) ? colids[e + u] : -1;
+#pragma unroll
+    for (int u = 0; u < kU; u++)
+      if (j[u] >= batch_lo) pj[u] = pold[j[u]];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      if (j[u] < batch_lo) continue;  // moved earlier in this iteration, or past the row end
+      bh_attract(pj[u], pv, W, hx, lx, hy, ly);
+    }
+  }
+  return make_float4(hx, hy, lx, ly);
+}
+
+// Unit-step update (algorithms.cpp:1062-1066) from the float-float force:
+// FP32 unit vector, FP64 only when |f|^2 leaves the FP32 range; |f| = 0
+// leaves the point where it is.
+__device__ __forceinline__ float2 bh_step(float2 pi, float hx, float lx, float hy, float ly, float step) {
+  const float fxf = hx + lx, fyf = hy + ly;
+  float2 np = pi;
+  const float m2 = fmaf(fxf, fxf, fyf * fyf);
+  if (m2 >= 1.17549435e-38f && m2 <= 3.0e38f) {
+    const float rm = rsqrt_approx(m2);
+    np.x = fmaf(step, fxf * rm, pi.x);
+    np.y = fmaf(step, fyf * rm, pi.y);
+  } else if (fxf != 0.f || fyf != 0.f) {
+    const double fx = (double)hx + (double)lx, fy = (double)hy + (double)ly;
+    const double mag = sqrt(fx * fx + fy * fy);
+    np.x = (float)((double)pi.x + (fx / mag) * (double)step);
+    np.y = (float)((double)pi.y + (fy / mag) * (double)step);
+  }
+  return np;
+}
+
+}  // namespace bl

@@ -175,6 +175,10 @@ struct Scratch {
 
 }  // namespace bl
 
+namespace bl {
+struct BatchedState;
+}
+
 struct bl_ctx {
   int device = 0;
   int num_sms = 0;
@@ -204,6 +208,7 @@ struct bl_ctx {
   long long timed_count = 0;
   cudaEvent_t run_ev[2] = {nullptr, nullptr};
   double last_run_ms = 0.0;
+  bl::BatchedState *batched = nullptr;  // many-graph layout (batched.cu)
 };
 
 // ---- helpers implemented in api.cu ---------------------------------------
@@ -233,6 +238,10 @@ int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_en
 int bh_canonical_tree(bl_ctx *ctx, int cap, int *lo, int *hi, int *depth, int *nchild,
                       double *centroid);
 const LevelSchedule *level_schedule(bl_ctx *ctx, int batch);
+void cursor_neighbours(int n, const std::vector<int> &rp, const std::vector<int> &ci, std::vector<int> &erp,
+                       std::vector<int> &eci);
+struct BatchedState;
+void batched_free(BatchedState *b);
 int energy_reduce(bl_ctx *ctx, double *out_host);
 int scan_exclusive_int(bl_ctx *ctx, const int *in, int *out, int n);
 }  // namespace bl

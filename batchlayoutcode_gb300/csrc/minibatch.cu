@@ -32,7 +32,7 @@
 #include <mutex>
 
 #include "../../include/batchlayout_gb300.h"
-#include "bl_internal.cuh"
+#include "bl_device.cuh"
 
 namespace bl {
 namespace {
@@ -82,27 +82,6 @@ struct MinibatchArgs {
   double engt;
   long long max_loops;
 };
-
-__device__ __forceinline__ void rep_pair(float xs, float ys, float xi, float yi, float &fx,
-                                         float &fy) {
-  const float dx = xs - xi, dy = ys - yi;
-  const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
-  const float r = rcp_approx(d2);
-  fx = fmaf(-dx, r, fx);
-  fy = fmaf(-dy, r, fy);
-}
-
-// Attraction of a matched neighbour, FP32 (algorithms.cpp:759 FR, :912 LinLog, :985 FA).
-__device__ __forceinline__ void attract_pair(int model, float W, float xs, float ys, float xi, float yi,
-                                             float &fx, float &fy) {
-  const float dx = xs - xi, dy = ys - yi;
-  float sc;
-  if (model == MODEL_FR) sc = W * sqrtf(fmaf(dx, dx, dy * dy));
-  else if (model == MODEL_LINLOG) sc = log2f(1.0f + W * sqrtf(fmaf(dx, dx, dy * dy)));
-  else sc = W;
-  fx = fmaf(dx, sc, fx);
-  fy = fmaf(dy, sc, fy);
-}
 
 // The reference's kindex cursor (algorithms.cpp:746,758-762) restricted to
 // this block's slice: the target's matched neighbours inside [slo, shi) are
@@ -198,15 +177,6 @@ __device__ __noinline__ void correct_neighbours(const MinibatchArgs &a, Cursor c
   }
 }
 
-// Compensated float-float accumulation (Knuth's TwoSum).
-__device__ __forceinline__ void ff_add(float &hi, float &lo, float t) {
-  const float sum = hi + t;
-  const float bb = sum - hi;
-  const float err = (hi - (sum - bb)) + (t - bb);
-  hi = sum;
-  lo += err;
-}
-
 // Slice of sources owned by block s: [lo, hi).
 __device__ __forceinline__ void slice_of(int n, int grid, int s, int &lo, int &hi) {
   lo = (int)(((long long)n * s) / grid);
@@ -253,7 +223,7 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
   };
   __shared__ double red[kWarps];
 
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x;
   const int grp = tid / kGroup, gl = tid % kGroup;
 
   for (int k = tid; k < slen; k += kThreads) slice[k] = a.pos[sbase + k];

@@ -169,6 +169,35 @@ def write_initf(xy: np.ndarray, path: str) -> None:
         f.write("".join(f"{x!r} {y!r} {i + 1}\n" for i, (x, y) in enumerate(xy.tolist())))
 
 
+def batched_mix(num_graphs: int = 2048, lo: int = 200, hi: int = 20000, seed: int = 1,
+                bh_min_vertices: int = 5000):
+    """Many small graphs for the batched launch: sizes log-uniform in [lo, hi],
+    a third each of triangulated grids, random geometric graphs (mean degree 6)
+    and Chung-Lu graphs (exponent 2.5, mean degree 8), each with its own
+    seeded disc initialisation; algo 2 below `bh_min_vertices` vertices and 4
+    from there.  The largest-component step can shrink a graph below its
+    drawn size.  -> (list of Graph, list of float32 (n, 2) arrays, algo array)"""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(math.log(lo), math.log(hi), size=num_graphs))
+    graphs, xys = [], []
+    for g in range(num_graphs):
+        n = max(2, int(round(sizes[g])))
+        kind = g % 3
+        if kind == 0:
+            r = max(2, int(round(math.sqrt(n))))
+            c = max(1, int(round(n / r)))
+            gr = grid_triangulated(r, c)
+        elif kind == 1:
+            gr = random_geometric(n, 6.0, seed=seed * 100003 + g)
+        else:
+            gr = chung_lu(n, 2.5, 8.0, seed=seed * 100003 + g)
+            gr.values = None
+        graphs.append(gr)
+        xys.append(init_disc(gr.n, seed=seed * 100003 + g))
+    algo = np.array([2 if gr.n < bh_min_vertices else 4 for gr in graphs], np.int32)
+    return graphs, xys, algo
+
+
 def workload(name: str, seed: int = 1):
     """Named workloads with their sizes: returns (graph, initial float32 xy)."""
     if name == "grid64":

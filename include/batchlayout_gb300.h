@@ -164,6 +164,50 @@ int bl_last_kernel_time(bl_ctx *ctx, const char *kernel, double *ms);
 /* Number of kernels this library launched since the context was created. */
 long long bl_kernel_launches(const bl_ctx *ctx);
 
+/* ---- many graphs in one launch ----------------------------------------------- */
+
+/* No counterpart in the reference, which lays out one graph per process
+ * (Test/BatchLayout.cpp:56-182, one algorithms object per run).  A batch of
+ * independent graphs is laid out by one persistent kernel (a device work
+ * queue, one block per graph, largest graph first), replayed as a CUDA graph.
+ * Each graph uses the reference's per-graph semantics: algo 2, 3 or 8 as
+ * cacheBlockingminiBatchForceDirectedAlgorithm / LinLog / FA
+ * (sample/algorithms.cpp:715-794, 874-1018; all coordinates of the graph in
+ * one block's shared memory, so these graphs are limited to about 26k
+ * vertices), algo 4 as BarnesHutApproximation (:1020-1083) with the same bits
+ * as bl_barnes_hut_iteration.  Every graph starts from the coordinates given
+ * and runs `iterations` iterations with STEP = 1 at the start; energy is the
+ * reference's ENERGY of its last iteration. */
+
+/* Context without a graph, for the batched calls (free with bl_destroy). */
+bl_ctx *bl_batch_create(int device);
+/* Upload the graphs.  Graph g has vertex_offset[g+1] - vertex_offset[g]
+ * vertices (vertex_offset[0] = 0); its CSR is rowptr[vertex_offset[g] + g ..
+ * vertex_offset[g+1] + g] (n+1 entries starting at 0) over
+ * colids[edge_offset[g] .. edge_offset[g+1]) with local vertex ids, as
+ * SetInputMatricesAsCSR builds it (sample/commonutility.h:26-54); algo[g] is
+ * 2, 3, 4 or 8; xy holds 2 * vertex_offset[num_graphs] doubles (x, y per
+ * vertex) of starting coordinates. */
+int bl_batched_prepare(bl_ctx *ctx, int num_graphs, const int *vertex_offset, const long long *edge_offset,
+                       const int *rowptr, const int *colids, const int *algo, const double *xy);
+/* Lay out every prepared graph from its starting coordinates (repeatable).
+ * The first run of a prepared set autotunes the source split of the
+ * minibatch graphs per size bucket; *seconds_out = device time of the run. */
+int bl_batched_run(bl_ctx *ctx, int iterations, int batch, double theta, double weight, double *seconds_out);
+/* Coordinates after the last run (2 * total vertices doubles, either may be
+ * NULL) and the energy of each graph's last iteration. */
+int bl_batched_result(bl_ctx *ctx, double *xy, double *energy);
+/* prepare + run + result in one call; xy is read and overwritten. */
+int bl_batched_layout(bl_ctx *ctx, int num_graphs, const int *vertex_offset, const long long *edge_offset,
+                      const int *rowptr, const int *colids, const int *algo, double *xy, int iterations, int batch,
+                      double theta, double weight, double *energy_out, double *seconds_out);
+/* Source ranges per target the autotuner chose for minibatch graphs below 512,
+ * below 2048 and from 2048 vertices (0 = no graph in that bucket). */
+int bl_batched_parts(const bl_ctx *ctx, int *parts3);
+/* Fix those choices (1, 2 or 4; 0 = autotune) for the next runs of the
+ * prepared set, e.g. to reproduce a run bit for bit. */
+int bl_batched_set_parts(bl_ctx *ctx, const int *parts3);
+
 /* ---- allocation-free variant ------------------------------------------------ */
 
 /* No counterpart in the reference.  One minibatch iteration (as
