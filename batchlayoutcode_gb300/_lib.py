@@ -25,6 +25,7 @@ EXPORTS = (
     "bl_kernel_launches", "bl_last_run_ms", "bl_random_coordinates", "bl_greedy_coordinates", "bl_write_coordinates",
     "bl_minibatch_iteration_noalloc", "bl_batch_create", "bl_batched_prepare", "bl_batched_run",
     "bl_batched_result", "bl_batched_layout", "bl_batched_parts", "bl_batched_set_parts",
+    "bl_batched_graph_cycles",
 )
 
 _lib = None
@@ -90,6 +91,7 @@ def load() -> C.CDLL:
                                     dp]),
         "bl_batched_parts": (i32, [vp, ip]),
         "bl_batched_set_parts": (i32, [vp, ip]),
+        "bl_batched_graph_cycles": (i32, [vp, C.POINTER(C.c_ulonglong)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -383,6 +385,12 @@ class BatchedLayout:
         """Source ranges per target chosen for minibatch graphs (< 512, < 2048, >= 2048 vertices)."""
         out = np.zeros(3, np.int32)
         self._check(self._L.bl_batched_parts(self._ctx, _ip(out)))
+        return out
+
+    def graph_cycles(self) -> np.ndarray:
+        """SM cycles the block spent on each graph in the last run."""
+        out = np.zeros(len(self.sizes), np.uint64)
+        self._check(self._L.bl_batched_graph_cycles(self._ctx, out.ctypes.data_as(C.POINTER(C.c_ulonglong))))
         return out
 
     def set_parts(self, parts3):

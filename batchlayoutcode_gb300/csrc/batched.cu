@@ -930,7 +930,7 @@ int bl_batched_run(bl_ctx *ctx, int iterations, int batch, double theta, double 
     B->graph = nullptr;
     BL_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     const long long before = ctx->launches;
-    const int rc = batched_launch(ctx, *B, B->num_graphs, B->d_order, nullptr, iterations);
+    const int rc = batched_launch(ctx, *B, B->num_graphs, B->d_order, B->d_cycles, iterations);
     cudaGraph_t graph = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
     ctx->launches = before;  // counted when the graph runs
@@ -985,6 +985,16 @@ int bl_batched_layout(bl_ctx *ctx, int num_graphs, const int *vertex_offset, con
   if (int rc = bl_batched_prepare(ctx, num_graphs, vertex_offset, edge_offset, rowptr, colids, algo, xy)) return rc;
   if (int rc = bl_batched_run(ctx, iterations, batch, theta, weight, seconds_out)) return rc;
   return bl_batched_result(ctx, xy, energy_out);
+}
+
+int bl_batched_graph_cycles(bl_ctx *ctx, unsigned long long *cycles) {
+  if (!ctx || !cycles) return BL_ERR_ARG;
+  if (!ctx->batched) return bl_fail(ctx, BL_ERR_STATE, "bl_batched_graph_cycles before bl_batched_prepare");
+  BL_CUDA(ctx, cudaSetDevice(ctx->device));
+  BL_CUDA(ctx, cudaMemcpyAsync(cycles, ctx->batched->d_cycles, sizeof(unsigned long long) * ctx->batched->num_graphs,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return BL_OK;
 }
 
 int bl_batched_set_parts(bl_ctx *ctx, const int *parts3) {

@@ -51,6 +51,12 @@ WORKLOADS = {
                              "largest component; disc init; algo 2 (all-pairs minibatch), batch 256"),
     "grid64": dict(algo=2, batch=256, theta=1.2,
                    desc="64x64 triangulated grid (4,096 vertices, 12,033 edges); disc init; algo 2, batch 256"),
+    "batched2048": dict(algo="batched", batch=256, theta=1.2, iterations=300,
+                        desc="2,048 graphs, sizes log-uniform in 200-20,000 vertices, a third each of triangulated "
+                             "grids, random geometric graphs (mean degree 6) and Chung-Lu graphs (exponent 2.5, "
+                             "mean degree 8), disc init per graph; 300 iterations of algo 2 below 5,000 vertices "
+                             "and algo 4 (bht 1.2) from there, batch 256; one persistent launch replayed as a "
+                             "CUDA graph"),
 }
 KERNEL_FOR_ALGO = {4: "traverse_kernel", 2: "minibatch_kernel", 3: "minibatch_kernel", 8: "minibatch_kernel"}
 
@@ -159,6 +165,53 @@ def load_workload(name: str):
     return G.cached_workload(name)
 
 
+def load_batched(seed: int = 1):
+    """The 2,048-graph mix, cached as one .npz of concatenated arrays."""
+    import numpy as np
+    from batchlayoutcode_gb300 import graphs as G
+    cache = os.path.join(ROOT, "batchlayoutcode_gb300", "_build", "workloads", f"batched2048_s{seed}.npz")
+    if os.path.exists(cache):
+        with np.load(cache) as z:
+            vo, eo, rp, ci, xy, algo = (z[k] for k in ("vertex_offset", "edge_offset", "rowptr", "colids", "xy",
+                                                       "algo"))
+        graphs = [(rp[vo[k] + k: vo[k + 1] + k + 1], ci[eo[k]:eo[k + 1]]) for k in range(vo.shape[0] - 1)]
+        xys = [xy[vo[k]:vo[k + 1]] for k in range(vo.shape[0] - 1)]
+        return graphs, xys, algo
+    gs, xys, algo = G.batched_mix(2048, 200, 20000, seed)
+    graphs = [(g.rowptr, g.colids) for g in gs]
+    vo = np.zeros(len(gs) + 1, np.int64)
+    vo[1:] = np.cumsum([g.n for g in gs])
+    eo = np.zeros(len(gs) + 1, np.int64)
+    eo[1:] = np.cumsum([g.colids.shape[0] for g in gs])
+    os.makedirs(os.path.dirname(cache), exist_ok=True)
+    np.savez(cache, vertex_offset=vo, edge_offset=eo, rowptr=np.concatenate([g.rowptr for g in gs]),
+             colids=np.concatenate([g.colids for g in gs]), xy=np.concatenate(xys), algo=algo)
+    return graphs, xys, algo
+
+
+def batched_sample(graphs, algo, iterations):
+    """Every 64th graph of the size-sorted mix (32 graphs spanning the size
+    range) at all iterations: 10-30 s of CPU work."""
+    import numpy as np
+    order = np.argsort([len(rp) for rp, _ in graphs])
+    pick = order[32::64]
+    return [int(k) for k in pick], iterations
+
+
+def cpu_baseline_batched(graphs, xys, algo, w, threads=None):
+    import oracle
+    pick, it = batched_sample(graphs, algo, w["iterations"])
+    t0 = time.perf_counter()
+    vi = 0
+    for k in pick:
+        rp, ci = graphs[k]
+        oracle.layout(int(algo[k]), rp, ci, xys[k].astype("float64"), it, w["batch"], w["theta"],
+                      nthreads=threads, fast=True)
+        vi += (len(rp) - 1) * it
+    dt = time.perf_counter() - t0
+    return vi / dt, dt, len(pick), it
+
+
 def cpu_baseline_port(g, xy, w, iters: int, threads: int | None = None):
     import oracle
     t0 = time.perf_counter()
@@ -219,6 +272,177 @@ def run_reference(args, w, g, xy):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_batched(args, w):
+    """The reference lays out one graph per process: run its binary (else the
+    port) graph by graph over the bounded sample with all host threads."""
+    graphs, xys, algo = load_batched()
+    cores = os.cpu_count() or 1
+    pick, it = batched_sample(graphs, algo, w["iterations"])
+    ref_bin = os.path.join(ROOT, "oracle", "_ref", "BatchLayout")
+    value, kind, sample = None, "port", None
+    if os.path.exists(ref_bin) and os.access(ref_bin, os.X_OK):
+        try:
+            from batchlayoutcode_gb300 import graphs as G
+            secs, vi = 0.0, 0
+            with tempfile.TemporaryDirectory() as td:
+                for k in pick:
+                    rp, ci = graphs[k]
+                    g = G.Graph(n=len(rp) - 1, rowptr=rp, colids=ci)
+                    mtx, initf = os.path.join(td, "w.mtx"), os.path.join(td, "w.initf")
+                    G.write_mtx(g, mtx)
+                    G.write_initf(xys[k], initf)
+                    out = subprocess.run([ref_bin, "-input", mtx, "-output", td + "/", "-iter", str(it), "-algo",
+                                          str(int(algo[k])), "-batch", str(w["batch"]), "-bht", str(w["theta"]),
+                                          "-initf", initf, "-threads", str(cores)], cwd=td, capture_output=True,
+                                         text=True, timeout=1800)
+                    m = re.search(r"Wall time required:([0-9.eE+-]+)", out.stdout)
+                    if out.returncode != 0 or not m:
+                        raise subprocess.SubprocessError("reference run failed")
+                    secs += float(m.group(1))
+                    vi += g.n * it
+            value, kind = vi / secs, "reference"
+            sample = (f"{len(pick)} graphs of the mix (every 64th by size) x {it} iterations, one reference "
+                      f"process per graph (binary built from source, stock flags), summed reported wall times")
+        except (OSError, subprocess.SubprocessError):
+            value = None
+    if value is None:
+        value, secs, npick, it = cpu_baseline_batched(graphs, xys, algo, w, cores)
+        sample = (f"{npick} graphs of the mix (every 64th by size) x {it} iterations with the FP64 port "
+                  f"(oracle/oracle.cpp, reference Makefile optimisation flags), {cores} OpenMP threads")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{args.workload}: {w['desc']}"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_batched(args, w, ws, rank, local):
+    """One step = the whole batched layout (every graph, all iterations)."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    device = local if ws > 1 else 0
+    import batchlayoutcode_gb300 as B
+    B.build()
+    graphs, xys, algo = load_batched()
+    iters, batch, theta = w["iterations"], w["batch"], w["theta"]
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, secs, npick, it = cpu_baseline_batched(graphs, xys, algo, w)
+        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"{npick} graphs of the mix (every 64th by size) x {it} iterations from the same starts, "
+                         f"FP64 port (oracle/oracle.cpp) with the reference Makefile's optimisation flags, "
+                         f"{os.cpu_count()} OpenMP threads, {secs:.1f} s"}
+    bl = B.BatchedLayout(graphs, algo, xys, device=device)
+    nv = int(bl.vertex_offset[-1])
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
+    for _ in range(args.warmup):
+        bl.run(iters, batch, theta)
+    launches0 = bl.kernel_launches()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    times = []
+    with Clocks(device) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            times.append(bl.run(iters, batch, theta))
+    torch.cuda.synchronize()
+    cyc = bl.graph_cycles().astype(np.float64)
+    launches = bl.kernel_launches() - launches0
+    total_s = sum(times)
+    if dist:
+        t = torch.tensor([total_s], device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = ws * nv * iters * args.steps / total_s
+    clocks = clk.summary()
+    sizes = bl.sizes
+    small = algo != 4
+    pairs = float(np.sum(sizes[small].astype(np.float64) ** 2)) * iters
+    avg_s = total_s / args.steps
+    sm_mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
+    peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    achieved = 10.0 * pairs / avg_s / 1e12
+    roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "traffic": traffic_from_profile("batched_kernel", args.workload), "kernel": "batched_kernel",
+            "kernel_ms_per_launch": avg_s * 1e3, "launches": args.steps,
+            "algorithmic_flops_per_launch": 10.0 * pairs,
+            "note": "flops of the minibatch graphs' pair sweeps only (10 per pair and iteration); the "
+                    "Barnes-Hut graphs' time is in the denominator, so this is a lower bound",
+            "peak_source": "nominal FP32 FMA peak: 152 SMs x 128 lanes x 2 flops x max SM clock"}
+    # end to end through the C ABI: host arrays in pinned memory, upload,
+    # run, read back, every step
+    L = bl._L
+
+    def pinned(a, dtype):
+        t = torch.empty(a.shape, dtype=dtype, pin_memory=True)
+        t.copy_(torch.from_numpy(np.ascontiguousarray(a)))
+        return t
+    h_vo = pinned(bl.vertex_offset, torch.int32)
+    h_eo = pinned(bl.edge_offset, torch.int64)
+    h_rp = pinned(bl.rowptr, torch.int32)
+    h_ci = pinned(bl.colids, torch.int32)
+    h_al = pinned(bl.algo, torch.int32)
+    h_xy = torch.empty((nv, 2), dtype=torch.float64, pin_memory=True)
+    h_e = torch.empty(len(sizes), dtype=torch.float64, pin_memory=True)
+    ip = C.POINTER(C.c_int)
+    dp = C.POINTER(C.c_double)
+    ctx = L.bl_batch_create(device)
+    e2e_steps = max(3, min(args.steps, 5))
+    secs = C.c_double()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        h_xy.copy_(torch.from_numpy(bl.xy0))
+        rc = L.bl_batched_layout(ctx, len(sizes), C.cast(h_vo.data_ptr(), ip),
+                                 C.cast(h_eo.data_ptr(), C.POINTER(C.c_longlong)), C.cast(h_rp.data_ptr(), ip),
+                                 C.cast(h_ci.data_ptr(), ip), C.cast(h_al.data_ptr(), ip),
+                                 C.cast(h_xy.data_ptr(), dp), iters, batch, theta, 1.0,
+                                 C.cast(h_e.data_ptr(), dp), C.byref(secs))
+        if rc != 0:
+            raise RuntimeError(L.bl_last_error(ctx).decode())
+    e2e_s = time.perf_counter() - t0
+    L.bl_destroy(ctx)
+    h2d = 16 * nv + 4 * (len(bl.rowptr) + len(bl.colids) + 2 * len(sizes)) + 8 * len(sizes)
+    e2e = {"value": ws * nv * iters * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": 16 * nv + 8 * len(sizes), "steps": e2e_steps,
+           "note": "bl_batched_layout per step: host preparation, upload, autotuning, the launch, read-back"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{args.workload}: {w['desc']}", "graphs": len(sizes), "vertices": nv,
+                       "minibatch_graphs": int(small.sum()), "barnes_hut_graphs": int((~small).sum()),
+                       "step": f"one batched layout: {iters} iterations of every graph",
+                       "l2": "flushed before every timed step (256 MB write)",
+                       "autotuned_parts": bl.parts().tolist(),
+                       "block_ms": {"max_minibatch_graph": float(cyc[small].max() / sm_mhz / 1e3),
+                                    "max_barnes_hut_graph": float(cyc[~small].max() / sm_mhz / 1e3)
+                                    if (~small).any() else 0.0,
+                                    "sum_minibatch": float(cyc[small].sum() / sm_mhz / 1e3),
+                                    "sum_barnes_hut": float(cyc[~small].sum() / sm_mhz / 1e3),
+                                    "note": "clock64 cycles per graph / max SM clock"},
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    bl.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -235,8 +459,14 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
+        if w["algo"] == "batched":
+            run_reference_batched(args, w)
+            return
         g, xy = load_workload(args.workload)
         run_reference(args, w, g, xy)
+        return
+    if w["algo"] == "batched":
+        run_batched(args, w, ws, rank, local)
         return
 
     import numpy as np

@@ -204,6 +204,9 @@ int bl_batched_layout(bl_ctx *ctx, int num_graphs, const int *vertex_offset, con
 /* Source ranges per target the autotuner chose for minibatch graphs below 512,
  * below 2048 and from 2048 vertices (0 = no graph in that bucket). */
 int bl_batched_parts(const bl_ctx *ctx, int *parts3);
+/* SM clock cycles (clock64) the block spent on each graph in the last run:
+ * the load balance of the launch (num_graphs values). */
+int bl_batched_graph_cycles(bl_ctx *ctx, unsigned long long *cycles);
 /* Fix those choices (1, 2 or 4; 0 = autotune) for the next runs of the
  * prepared set, e.g. to reproduce a run bit for bit. */
 int bl_batched_set_parts(bl_ctx *ctx, const int *parts3);
