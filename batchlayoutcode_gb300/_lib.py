@@ -25,7 +25,7 @@ EXPORTS = (
     "bl_kernel_launches", "bl_last_run_ms", "bl_random_coordinates", "bl_greedy_coordinates", "bl_write_coordinates",
     "bl_minibatch_iteration_noalloc", "bl_batch_create", "bl_batched_prepare", "bl_batched_run",
     "bl_batched_result", "bl_batched_layout", "bl_batched_parts", "bl_batched_set_parts",
-    "bl_batched_graph_cycles",
+    "bl_batched_graph_cycles", "bl_mpnn_set_params", "bl_mpnn_get_params", "bl_mpnn_run",
 )
 
 _lib = None
@@ -92,6 +92,11 @@ def load() -> C.CDLL:
         "bl_batched_parts": (i32, [vp, ip]),
         "bl_batched_set_parts": (i32, [vp, ip]),
         "bl_batched_graph_cycles": (i32, [vp, C.POINTER(C.c_ulonglong)]),
+        "bl_mpnn_set_params": (i32, [vp, C.POINTER(C.c_float)]),
+        "bl_mpnn_get_params": (i32, [vp, C.POINTER(C.c_float)]),
+        "bl_mpnn_run": (i32, [vp, i32, ip, ip, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                              C.POINTER(C.c_float), C.POINTER(C.c_ushort), C.POINTER(C.c_double),
+                              C.POINTER(C.c_float)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -399,6 +404,77 @@ class BatchedLayout:
 
     def kernel_launches(self) -> int:
         return int(self._L.bl_kernel_launches(self._ctx))
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._L.bl_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+MPNN_PARAMS = 18754
+MPNN_FEATURES = 16
+
+
+def _fp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Mpnn:
+    """The learned initializer's network on the GPU (bl_mpnn_*)."""
+
+    def __init__(self, params=None, device: int = 0):
+        L = load()
+        self._L = L
+        ctx = L.bl_batch_create(device)
+        if not ctx:
+            raise BatchLayoutError(-2, "bl_batch_create failed")
+        self._ctx = ctx
+        if params is not None:
+            self.set_params(params)
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise BatchLayoutError(rc, self._L.bl_last_error(self._ctx).decode())
+
+    def set_params(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        assert p.shape == (MPNN_PARAMS,)
+        self._check(self._L.bl_mpnn_set_params(self._ctx, _fp(p)))
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(MPNN_PARAMS, np.float32)
+        self._check(self._L.bl_mpnn_get_params(self._ctx, _fp(p)))
+        return p
+
+    def run(self, rowptr, colids, features, target=None, vweight=None, want_h=False):
+        """-> dict(xy, h (3, n, 64) BF16 bits or None, loss, grad)."""
+        rp = np.ascontiguousarray(rowptr, np.int32)
+        ci = np.ascontiguousarray(colids, np.int32) if len(colids) else np.zeros(1, np.int32)
+        n = rp.shape[0] - 1
+        f = np.ascontiguousarray(features, np.float32).reshape(n, MPNN_FEATURES)
+        xy = np.zeros((n, 2), np.float32)
+        h = np.zeros((3, n, 64), np.uint16) if want_h else None
+        loss = C.c_double()
+        grad = np.zeros(MPNN_PARAMS, np.float32)
+        t = np.ascontiguousarray(target, np.float32).reshape(n, 2) if target is not None else None
+        w = np.ascontiguousarray(vweight, np.float32) if vweight is not None else None
+        self._check(self._L.bl_mpnn_run(self._ctx, n, _ip(rp), _ip(ci), _fp(f), _fp(t) if t is not None else None,
+                                        _fp(w) if w is not None else None, _fp(xy),
+                                        h.ctypes.data_as(C.POINTER(C.c_ushort)) if h is not None else None,
+                                        C.byref(loss), _fp(grad)))
+        return dict(xy=xy, h=h, loss=loss.value if t is not None else None, grad=grad if t is not None else None)
 
     def close(self):
         if getattr(self, "_ctx", None):

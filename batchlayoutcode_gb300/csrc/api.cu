@@ -36,6 +36,7 @@ int bl_check_status(bl_ctx *ctx) {
   const char *what = st.code == DEV_TIMEOUT_GRID_BARRIER ? "grid barrier timed out"
                      : st.code == DEV_TIMEOUT_TREE        ? "tree build wait timed out"
                      : st.code == DEV_FORCE_RANGE         ? "force beyond the fixed-point range (coincident vertices?)"
+                     : st.code == DEV_TIMEOUT_MMA         ? "tensor-core MMA completion wait timed out"
                                                           : "device error";
   cudaMemset(ctx->s.status, 0, sizeof(DevStatus));
   return bl_fail(ctx, BL_ERR_DEVICE_TIMEOUT,
@@ -139,6 +140,8 @@ void free_ctx(bl_ctx *c) {
   }
   bl::batched_free(c->batched);
   c->batched = nullptr;
+  bl::mpnn_free(c->mpnn);
+  c->mpnn = nullptr;
   for (auto ev : c->ev_pool) cudaEventDestroy(ev);
   for (auto ev : c->run_ev)
     if (ev) cudaEventDestroy(ev);

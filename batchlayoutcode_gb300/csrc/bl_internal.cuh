@@ -19,6 +19,7 @@ enum : unsigned int {
   DEV_TIMEOUT_TREE = 2,
   DEV_BAD_INDEX = 3,
   DEV_FORCE_RANGE = 4,
+  DEV_TIMEOUT_MMA = 5,
 };
 
 struct DevStatus {
@@ -177,6 +178,7 @@ struct Scratch {
 
 namespace bl {
 struct BatchedState;
+struct MpnnState;
 }
 
 struct bl_ctx {
@@ -209,6 +211,7 @@ struct bl_ctx {
   cudaEvent_t run_ev[2] = {nullptr, nullptr};
   double last_run_ms = 0.0;
   bl::BatchedState *batched = nullptr;  // many-graph layout (batched.cu)
+  bl::MpnnState *mpnn = nullptr;        // learned initializer (mpnn.cu)
 };
 
 // ---- helpers implemented in api.cu ---------------------------------------
@@ -242,6 +245,7 @@ void cursor_neighbours(int n, const std::vector<int> &rp, const std::vector<int>
                        std::vector<int> &eci);
 struct BatchedState;
 void batched_free(BatchedState *b);
+void mpnn_free(MpnnState *m);
 int energy_reduce(bl_ctx *ctx, double *out_host);
 int scan_exclusive_int(bl_ctx *ctx, const int *in, int *out, int n);
 }  // namespace bl

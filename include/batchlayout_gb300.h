@@ -211,6 +211,33 @@ int bl_batched_graph_cycles(bl_ctx *ctx, unsigned long long *cycles);
  * prepared set, e.g. to reproduce a run bit for bit. */
 int bl_batched_set_parts(bl_ctx *ctx, const int *parts3);
 
+/* ---- learned initializer: the message-passing network ------------------------ */
+
+/* No counterpart in the reference (its initial layouts are random, greedy DFS
+ * or read from a file, sample/algorithms.cpp:16-119).  A 3-layer
+ * message-passing network (16 input features, 64 hidden, mean aggregation
+ * over the CSR neighbours, ReLU) with a linear 64 -> 2 readout predicts
+ * initial coordinates; BF16 weights and activations, FP32 accumulation on
+ * the tensor cores.  Parameters are one FP32 vector of BL_MPNN_PARAMS values:
+ * W1 (64 x 32), b1 (64), W2 (64 x 128), b2 (64), W3 (64 x 128), b3 (64),
+ * Wo (2 x 64), bo (2); row o of W_l holds the weights of output o over
+ * [own features | mean of the neighbours' features]. */
+#define BL_MPNN_PARAMS 18754
+#define BL_MPNN_FEATURES 16
+
+/* Load / read the parameters of the context's network (any context). */
+int bl_mpnn_set_params(bl_ctx *ctx, const float *params);
+int bl_mpnn_get_params(bl_ctx *ctx, float *params);
+/* One forward pass over a graph given as host arrays (CSR rowptr[n+1],
+ * colids, features[n*16] row-major): xy[2n] receives the predicted
+ * coordinates and, if h is not NULL, h[3*n*64] the BF16 activations of the
+ * three layers.  With target != NULL (2n values) and vweight (n values) the
+ * loss sum_v vweight[v] * |xy_v - target_v|^2 and its gradient with respect
+ * to the parameters (grad[BL_MPNN_PARAMS]) are computed as well. */
+int bl_mpnn_run(bl_ctx *ctx, int n, const int *rowptr, const int *colids, const float *features,
+                const float *target, const float *vweight, float *xy, unsigned short *h, double *loss,
+                float *grad);
+
 /* ---- allocation-free variant ------------------------------------------------ */
 
 /* No counterpart in the reference.  One minibatch iteration (as
