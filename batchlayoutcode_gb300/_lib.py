@@ -26,6 +26,7 @@ EXPORTS = (
     "bl_minibatch_iteration_noalloc", "bl_batch_create", "bl_batched_prepare", "bl_batched_run",
     "bl_batched_result", "bl_batched_layout", "bl_batched_parts", "bl_batched_set_parts",
     "bl_batched_graph_cycles", "bl_mpnn_set_params", "bl_mpnn_get_params", "bl_mpnn_run",
+    "bl_learned_features", "bl_learned_train", "bl_learned_init", "bl_learned_layout",
 )
 
 _lib = None
@@ -97,6 +98,11 @@ def load() -> C.CDLL:
         "bl_mpnn_run": (i32, [vp, i32, ip, ip, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                               C.POINTER(C.c_float), C.POINTER(C.c_ushort), C.POINTER(C.c_double),
                               C.POINTER(C.c_float)]),
+        "bl_learned_features": (i32, [vp, i32, ip, ip, i32, ip, C.POINTER(C.c_float), C.POINTER(C.c_ushort), ip]),
+        "bl_learned_train": (i32, [vp, i32, ip, C.POINTER(C.c_longlong), ip, ip, dp, i32, f64, i32,
+                                   C.POINTER(C.c_float), dp, dp]),
+        "bl_learned_init": (i32, [vp, C.POINTER(C.c_float), dp, i32]),
+        "bl_learned_layout": (i32, [vp, C.POINTER(C.c_float), dp, i32, i32, i32, f64, f64, f64, dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -336,6 +342,22 @@ class Algorithms:
     def kernel_launches(self) -> int:
         return int(self._L.bl_kernel_launches(self._ctx))
 
+    def learnedInit(self, params, scale_model, seed: int = 1):
+        """Coordinates predicted by the learned initializer (bl_learned_init)."""
+        p = np.ascontiguousarray(params, np.float32)
+        sm = np.ascontiguousarray(scale_model, np.float64)
+        self._check(self._L.bl_learned_init(self._ctx, _fp(p), _dp(sm), seed))
+
+    def learnedLayout(self, params, scale_model, max_iterations: int, target_energy: float, batch: int = 256,
+                      theta: float = 1.2, step0: float = 0.3, seed: int = 1) -> dict:
+        """bl_learned_layout: learned start + Barnes-Hut until target_energy (greedy fallback)."""
+        p = np.ascontiguousarray(params, np.float32)
+        sm = np.ascontiguousarray(scale_model, np.float64)
+        o = (C.c_double * 5)()
+        self._check(self._L.bl_learned_layout(self._ctx, _fp(p), _dp(sm), seed, max_iterations, batch, theta,
+                                              target_energy, step0, o))
+        return dict(energy=o[0], seconds=o[1], iterations=int(o[2]), fell_back=bool(o[3]), init_seconds=o[4])
+
 
 class BatchedLayout:
     """Many independent graphs laid out by one persistent launch (no
@@ -404,6 +426,22 @@ class BatchedLayout:
 
     def kernel_launches(self) -> int:
         return int(self._L.bl_kernel_launches(self._ctx))
+
+    def learnedInit(self, params, scale_model, seed: int = 1):
+        """Coordinates predicted by the learned initializer (bl_learned_init)."""
+        p = np.ascontiguousarray(params, np.float32)
+        sm = np.ascontiguousarray(scale_model, np.float64)
+        self._check(self._L.bl_learned_init(self._ctx, _fp(p), _dp(sm), seed))
+
+    def learnedLayout(self, params, scale_model, max_iterations: int, target_energy: float, batch: int = 256,
+                      theta: float = 1.2, step0: float = 0.3, seed: int = 1) -> dict:
+        """bl_learned_layout: learned start + Barnes-Hut until target_energy (greedy fallback)."""
+        p = np.ascontiguousarray(params, np.float32)
+        sm = np.ascontiguousarray(scale_model, np.float64)
+        o = (C.c_double * 5)()
+        self._check(self._L.bl_learned_layout(self._ctx, _fp(p), _dp(sm), seed, max_iterations, batch, theta,
+                                              target_energy, step0, o))
+        return dict(energy=o[0], seconds=o[1], iterations=int(o[2]), fell_back=bool(o[3]), init_seconds=o[4])
 
     def close(self):
         if getattr(self, "_ctx", None):
@@ -475,6 +513,39 @@ class Mpnn:
                                         h.ctypes.data_as(C.POINTER(C.c_ushort)) if h is not None else None,
                                         C.byref(loss), _fp(grad)))
         return dict(xy=xy, h=h, loss=loss.value if t is not None else None, grad=grad if t is not None else None)
+
+    def train(self, graphs, layouts, epochs: int, lr: float = 3e-3, seed: int = 1):
+        """bl_learned_train on [(rowptr, colids)] and their (n, 2) target layouts;
+        the context's parameters are the start.  -> (params, scale_model, loss history)."""
+        G = len(graphs)
+        vo = np.zeros(G + 1, np.int32)
+        vo[1:] = np.cumsum([len(rp) - 1 for rp, _ in graphs])
+        eo = np.zeros(G + 1, np.int64)
+        eo[1:] = np.cumsum([len(ci) for _, ci in graphs])
+        rp = np.ascontiguousarray(np.concatenate([np.asarray(r, np.int32) for r, _ in graphs]))
+        ci = np.ascontiguousarray(np.concatenate([np.asarray(c, np.int32) for _, c in graphs] + [np.zeros(1, np.int32)]))
+        lay = np.ascontiguousarray(np.concatenate([np.asarray(x, np.float64).reshape(-1, 2) for x in layouts]))
+        params = self.get_params()
+        sm = np.zeros(3)
+        hist = np.zeros(max(epochs, 1))
+        self._check(self._L.bl_learned_train(self._ctx, G, _ip(vo), eo.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                             _ip(rp), _ip(ci), _dp(lay), epochs, lr, seed, _fp(params), _dp(sm),
+                                             _dp(hist)))
+        return params, sm, hist[:epochs]
+
+    def features(self, rowptr, colids, seed: int = 1, pivots=None):
+        """-> (features (n, 16) float32, hop distances (n, 16) uint16, pivots (16,))."""
+        rp = np.ascontiguousarray(rowptr, np.int32)
+        ci = np.ascontiguousarray(colids, np.int32) if len(colids) else np.zeros(1, np.int32)
+        n = rp.shape[0] - 1
+        f = np.zeros((n, MPNN_FEATURES), np.float32)
+        d = np.zeros((n, 16), np.uint16)
+        pv = np.zeros(16, np.int32)
+        pin = np.ascontiguousarray(pivots, np.int32) if pivots is not None else None
+        self._check(self._L.bl_learned_features(self._ctx, n, _ip(rp), _ip(ci), seed,
+                                                _ip(pin) if pin is not None else None, _fp(f),
+                                                d.ctypes.data_as(C.POINTER(C.c_ushort)), _ip(pv)))
+        return f, d, pv
 
     def close(self):
         if getattr(self, "_ctx", None):

@@ -729,6 +729,11 @@ int mpnn_adam_step(bl_ctx *ctx, double lr) {
 
 int mpnn_prepare(bl_ctx *ctx, int n) { return ensure_mpnn(ctx, n); }
 
+__nv_bfloat16 *mpnn_input(bl_ctx *ctx) { return ctx->mpnn->x; }
+const float *mpnn_output(bl_ctx *ctx) { return ctx->mpnn->xy; }
+float *mpnn_targets(bl_ctx *ctx) { return ctx->mpnn->target; }
+float *mpnn_vweights(bl_ctx *ctx) { return ctx->mpnn->vweight; }
+
 int mpnn_set_params_device(bl_ctx *ctx, const float *h_params) {
   if (int rc = ensure_mpnn(ctx, 1)) return rc;
   MpnnState &m = *ctx->mpnn;

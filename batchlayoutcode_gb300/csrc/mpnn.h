@@ -1,6 +1,8 @@
 // mpnn.h -- host interface of the learned initializer's network (mpnn.cu).
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include "bl_internal.cuh"
 
 namespace bl {
@@ -18,5 +20,11 @@ int mpnn_forward(bl_ctx *ctx, int n, const int *d_rowptr, const int *d_colids, b
 int mpnn_backward(bl_ctx *ctx, int n, const int *d_rowptr, const int *d_colids);
 int mpnn_loss(bl_ctx *ctx, int n, double *loss);
 int mpnn_adam_step(bl_ctx *ctx, double lr);
+// device buffers of the prepared network: BF16 input features (n x 16),
+// output coordinates (n x 2), training targets (n x 2) and vertex weights (n)
+__nv_bfloat16 *mpnn_input(bl_ctx *ctx);
+const float *mpnn_output(bl_ctx *ctx);
+float *mpnn_targets(bl_ctx *ctx);
+float *mpnn_vweights(bl_ctx *ctx);
 
 }  // namespace bl

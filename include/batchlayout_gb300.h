@@ -238,6 +238,41 @@ int bl_mpnn_run(bl_ctx *ctx, int n, const int *rowptr, const int *colids, const 
                 const float *target, const float *vweight, float *xy, unsigned short *h, double *loss,
                 float *grad);
 
+/* Input features of the network for one graph (host arrays): multi-source
+ * BFS hop distances to 16 pivots (given, or drawn with splitmix64 from seed
+ * when pivots is NULL), pivot-MDS component scores 1-12 of the double-centred
+ * squared distances scaled to unit mean square of component 1, then
+ * log2(1+deg), 1/(1+deg), the neighbours' mean log2(1+deg) and log2(n)/20.
+ * features: n*16 floats; dist (optional): n*16 hop distances, 0xFFFF for an
+ * unreachable pivot; pivots_out (optional): the 16 pivots used. */
+int bl_learned_features(bl_ctx *ctx, int n, const int *rowptr, const int *colids, int seed, const int *pivots,
+                        float *features, unsigned short *dist, int *pivots_out);
+
+/* Train the network on graphs and their target layouts (what algo 4 produced
+ * for them): graphs as in bl_batched_prepare, layouts 2 * total vertices
+ * doubles.  The network learns the residual between each target, fitted to
+ * the graph's first two MDS components y by a similarity transform, and y.
+ * params holds the starting parameters and receives the trained ones;
+ * scale_model[3] receives {a, b, c} of log l = a + b log n + c log(mean
+ * degree), l the mean edge length of a target; loss_history (optional) one
+ * loss per epoch.  Full-batch Adam, cosine learning rate from lr, pivots
+ * drawn from seed + graph index. */
+int bl_learned_train(bl_ctx *ctx, int num_graphs, const int *vertex_offset, const long long *edge_offset,
+                     const int *rowptr, const int *colids, const double *layouts, int epochs, double lr, int seed,
+                     float *params, double *scale_model, double *loss_history);
+/* Replace the context's coordinates by the learned start for its graph (the
+ * learned counterpart of bl_init_dfs): y + network output, scaled to the mean
+ * edge length the scale model predicts. */
+int bl_learned_init(bl_ctx *ctx, const float *params, const double *scale_model, int seed);
+/* Learned start, then Barnes-Hut iterations (batch, theta; STEP from step0,
+ * times 0.999 per iteration, as :1070) until the energy of an iteration is at
+ * most target_energy or max_iterations ran; if the target was not reached,
+ * the plain run instead: greedy DFS start and max_iterations iterations from
+ * STEP = 1.  out[5] = {energy, wall seconds, refinement iterations, 1 if the
+ * plain run was used, seconds of the learned start}. */
+int bl_learned_layout(bl_ctx *ctx, const float *params, const double *scale_model, int seed, int max_iterations,
+                      int batch, double theta, double target_energy, double step0, double *out);
+
 /* ---- allocation-free variant ------------------------------------------------ */
 
 /* No counterpart in the reference.  One minibatch iteration (as

@@ -147,3 +147,70 @@ def init_params(seed: int = 0) -> np.ndarray:
     out.append(rng.normal(0.0, np.sqrt(1.0 / 64), size=128))
     out.append(np.zeros(2))
     return np.concatenate(out).astype(np.float32)
+
+
+# ---- input features (batchlayoutcode_gb300/csrc/features.cu) ----------------
+
+def splitmix64_pivots(n: int, seed: int, k: int = 16) -> np.ndarray:
+    """The device's pivot choice: splitmix64 draws modulo n, duplicates skipped."""
+    if n <= k:
+        return np.arange(k) % n
+    mask = (1 << 64) - 1
+    x = seed & mask
+    out = []
+    while len(out) < k:
+        x = (x + 0x9E3779B97F4A7C15) & mask
+        z = x
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & mask
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & mask
+        z ^= z >> 31
+        p = z % n
+        if p not in out:
+            out.append(p)
+    return np.array(out, np.int64)
+
+
+def hop_distances(rowptr, colids, pivots) -> np.ndarray:
+    """(n, 16) hop distances, -1 where unreachable (FP64 BFS by scipy)."""
+    from scipy.sparse import csr_matrix
+    from scipy.sparse.csgraph import shortest_path
+    rowptr = np.asarray(rowptr, np.int64)
+    n = rowptr.shape[0] - 1
+    A = csr_matrix((np.ones(rowptr[-1]), np.asarray(colids, np.int64)[:rowptr[-1]], rowptr), shape=(n, n))
+    D = shortest_path(A, unweighted=True, directed=False, indices=np.asarray(pivots)).T
+    return np.where(np.isinf(D), -1, D).astype(np.int64)
+
+
+def features(rowptr, colids, pivots):
+    """-> (features (n, 16) FP64, eigenvalues (16,), hop distances)."""
+    rowptr = np.asarray(rowptr, np.int64)
+    colids = np.asarray(colids, np.int64)
+    n = rowptr.shape[0] - 1
+    d = hop_distances(rowptr, colids, pivots).astype(np.float64)
+    for s in range(d.shape[1]):
+        col = d[:, s]
+        m = col[col >= 0].max() if np.any(col >= 0) else 0.0
+        col[col < 0] = m + 1
+    D2 = d * d
+    r = D2.mean(1)
+    c = D2.mean(0)
+    g = c.mean()
+    C = -0.5 * (D2 - r[:, None] - c[None, :] + g)
+    S = C.T @ C
+    lam, V = np.linalg.eigh(S)
+    order = np.argsort(-lam, kind="stable")
+    lam, V = lam[order], V[:, order]
+    for j in range(V.shape[1]):
+        arg = int(np.argmax(np.abs(V[:, j])))
+        if V[arg, j] < 0:
+            V[:, j] = -V[:, j]
+    Y = C @ V[:, :12]
+    Y = Y / np.sqrt(lam[0] / n) if lam[0] > 0 else Y * 0.0
+    deg = np.diff(rowptr).astype(np.float64)
+    ld = np.log2(1.0 + deg)
+    nb = np.zeros(n)
+    np.add.at(nb, np.repeat(np.arange(n), np.diff(rowptr)), ld[colids[:rowptr[-1]]])
+    nb = np.where(deg > 0, nb / np.maximum(deg, 1), 0.0)
+    F = np.concatenate([Y, ld[:, None], (1.0 / (1.0 + deg))[:, None], nb[:, None],
+                        np.full((n, 1), np.log2(n) / 20.0)], axis=1)
+    return F, lam, d

@@ -67,3 +67,22 @@ def test_params_round_trip(B):
     p = M.init_params(4)
     with B._lib.Mpnn(p) as net:
         assert np.array_equal(net.get_params(), p)
+
+
+def test_features_match_oracle(B):
+    from batchlayoutcode_gb300 import graphs as G
+    for g in (G.random_geometric(4000, 6.0, seed=3), G.chung_lu(3000, 2.5, 8.0, seed=4),
+              G.grid_triangulated(40, 55)):
+        with B._lib.Mpnn() as net:
+            f, d, piv = net.features(g.rowptr, g.colids, seed=11)
+        assert np.array_equal(piv, M.splitmix64_pivots(g.n, 11))
+        ref, lam, dref = M.features(g.rowptr, g.colids, piv)
+        dd = d.astype(np.int64)
+        dd[d == 0xFFFF] = -1
+        assert np.array_equal(dd, M.hop_distances(g.rowptr, g.colids, piv)), g.name
+        # components with a clear eigen-gap are determined; compare those
+        for j in range(12):
+            gap = min(abs(lam[j] - lam[j - 1]) if j > 0 else np.inf, abs(lam[j] - lam[j + 1])) / lam[0]
+            if gap > 1e-3:
+                assert rel(f[:, j], ref[:, j]) <= 1e-4, (g.name, j)
+        assert rel(f[:, 12:], ref[:, 12:]) <= 1e-6, g.name
