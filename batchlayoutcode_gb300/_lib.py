@@ -27,6 +27,7 @@ EXPORTS = (
     "bl_batched_result", "bl_batched_layout", "bl_batched_parts", "bl_batched_set_parts",
     "bl_batched_graph_cycles", "bl_mpnn_set_params", "bl_mpnn_get_params", "bl_mpnn_run",
     "bl_learned_features", "bl_learned_train", "bl_learned_init", "bl_learned_layout",
+    "bl_learned_load_model",
 )
 
 _lib = None
@@ -103,6 +104,7 @@ def load() -> C.CDLL:
                                    C.POINTER(C.c_float), dp, dp]),
         "bl_learned_init": (i32, [vp, C.POINTER(C.c_float), dp, i32]),
         "bl_learned_layout": (i32, [vp, C.POINTER(C.c_float), dp, i32, i32, i32, f64, f64, f64, dp]),
+        "bl_learned_load_model": (i32, [cp, C.POINTER(C.c_float), dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -26,6 +26,7 @@ static void helpmessage() {
   printf("-batch <int>, size of minibatch.\n");
   printf("-init <int>, any of 0 or 1, 1 - random initialization, 0 - greedy initialization.\n");
   printf("-initf <string>, this will overwrite -init and initialize coordinates from a given file.\n");
+  printf("-learned <string>, learned initialization with the model file given (overwrites -init and -initf).\n");
   printf("-iter <int>, number of iteration.\n");
   printf("-threads <int>, number of threads, default value is maximum available threads in the machine.\n");
   printf("-algo <int>, an integer among 0, 1, 2, 3, 4, 5 and 6.\n");
@@ -86,7 +87,7 @@ int main(int argc, char *argv[]) {
     if (strcmp(argv[p], "-input") == 0) inputfile = arg(p);
     if (strcmp(argv[p], "-output") == 0) outputfile = arg(p);
     if (strcmp(argv[p], "-batch") == 0) batchsize = atoi(arg(p));
-    if (strcmp(argv[p], "-init") == 0 && init != 2) {
+    if (strcmp(argv[p], "-init") == 0 && init != 2 && init != 3) {
       init = atoi(arg(p));
       if (init < 0 || init > 1) init = 1;
     }
@@ -94,9 +95,13 @@ int main(int argc, char *argv[]) {
     if (strcmp(argv[p], "-threads") == 0) numberOfThreads = atoi(arg(p));
     if (strcmp(argv[p], "-algo") == 0) algoOption = atoi(arg(p));
     if (strcmp(argv[p], "-bht") == 0) bhThreshold = atof(arg(p));
-    if (strcmp(argv[p], "-initf") == 0) {
+    if (strcmp(argv[p], "-initf") == 0 && init != 3) {
       initfile = arg(p);
       init = 2;
+    }
+    if (strcmp(argv[p], "-learned") == 0) {
+      initfile = arg(p);
+      init = 3;
     }
     if (strcmp(argv[p], "-engt") == 0) {
       energyThreshold = atof(arg(p));
@@ -114,6 +119,7 @@ int main(int argc, char *argv[]) {
   }
   if (init == 1) initname = "RANDOM";
   if (init == 2) initname = "FILE";
+  if (init == 3) initname = "LEARNED";
   banner();
   // SetInputMatricesAsCSR prints these lines (sample/commonutility.h:31-32, IO.h:72-150)
   std::cout << "Reading input matrices in text (ascii)... " << std::endl;

@@ -151,6 +151,16 @@ void free_ctx(bl_ctx *c) {
 int init_coordinates(bl_ctx *ctx) {
   if (ctx->init == 0) return bl_init_dfs(ctx);
   if (ctx->init == 2) return bl_file_initialization(ctx);
+  if (ctx->init == 3) {
+    // learned start from the model file in initfile (no reference counterpart)
+    std::vector<float> params(BL_MPNN_PARAMS);
+    double sm[3];
+    if (int rc = bl_learned_load_model(ctx->initfile.c_str(), params.data(), sm)) {
+      bl_fail(ctx, rc, std::string("cannot read model file ") + ctx->initfile);
+      return rc;
+    }
+    return bl_learned_init(ctx, params.data(), sm, 1);
+  }
   return bl_rand_init(ctx);
 }
 

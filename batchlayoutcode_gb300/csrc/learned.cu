@@ -22,6 +22,7 @@
 // above the target.
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -398,6 +399,41 @@ int bl_learned_train(bl_ctx *ctx, int num_graphs, const int *vertex_offset, cons
   cudaFree(d_ci);
   cudaFree(d_f);
   cudaFree(d_d);
+  return rc;
+}
+
+int bl_learned_load_model(const char *path, float *params, double *scale_model) {
+  if (!path || !params || !scale_model) return BL_ERR_ARG;
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return BL_ERR_IO;
+  char magic[8];
+  unsigned char cnt[4];
+  int rc = BL_OK;
+  if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, "BLMPNN01", 8) != 0 || std::fread(cnt, 1, 4, f) != 4)
+    rc = BL_ERR_IO;
+  // little-endian fields, read byte by byte so the host's byte order does not matter
+  const unsigned count = cnt[0] | (cnt[1] << 8) | (cnt[2] << 16) | ((unsigned)cnt[3] << 24);
+  if (!rc && count != (unsigned)bl::kMpnnParams) rc = BL_ERR_IO;
+  for (int i = 0; i < bl::kMpnnParams && !rc; i++) {
+    unsigned char b[4];
+    if (std::fread(b, 1, 4, f) != 4) {
+      rc = BL_ERR_IO;
+      break;
+    }
+    const uint32_t u = b[0] | (b[1] << 8) | (b[2] << 16) | ((uint32_t)b[3] << 24);
+    std::memcpy(&params[i], &u, 4);
+  }
+  for (int i = 0; i < 3 && !rc; i++) {
+    unsigned char b[8];
+    if (std::fread(b, 1, 8, f) != 8) {
+      rc = BL_ERR_IO;
+      break;
+    }
+    uint64_t u = 0;
+    for (int k = 7; k >= 0; k--) u = (u << 8) | b[k];
+    std::memcpy(&scale_model[i], &u, 8);
+  }
+  std::fclose(f);
   return rc;
 }
 

@@ -647,6 +647,7 @@ int mpnn_forward(bl_ctx *ctx, int n, const int *d_rowptr, const int *d_colids, b
   a.rowptr = d_rowptr;
   a.colids = d_colids;
   a.st = ctx->s.status;
+  bl_time_begin(ctx, "mpnn_forward");
   for (int l = 0; l < 3; l++) {
     a.hin = l == 0 ? m.x : m.h[l - 1];
     a.hout = m.h[l];
@@ -670,6 +671,7 @@ int mpnn_forward(bl_ctx *ctx, int n, const int *d_rowptr, const int *d_colids, b
     ctx->launches++;
     BL_CUDA(ctx, cudaGetLastError());
   }
+  bl_time_end(ctx, "mpnn_forward");
   return 0;
 }
 

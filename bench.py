@@ -272,6 +272,38 @@ def run_reference(args, w, g, xy):
     print(json.dumps(line), flush=True)
 
 
+def time_to_energy(B, g, w, iterations: int = 600):
+    """Seconds to the plain run's final energy (+0.5%): the plain GPU run
+    (greedy DFS start, `iterations` Barnes-Hut iterations from STEP 1) against
+    the learned start refined by Barnes-Hut until that energy (greedy
+    fallback), and the same pipeline with a zero network (pivot-MDS shape)."""
+    import numpy as np
+    from batchlayoutcode_gb300 import learned as LR
+    params, sm = LR.load_model()
+    with B.Algorithms(g.rowptr, g.colids, init=0) as a:
+        e_plain, plain_s = a.BarnesHutApproximation(iterations, 0, w["batch"], w["theta"], 0)
+    target = e_plain * 1.005
+    with B.Algorithms(g.rowptr, g.colids, init=0) as a:
+        a.kernel_time("mpnn_forward")
+        r = a.learnedLayout(params, sm, iterations, target, w["batch"], w["theta"], LR.STEP0)
+        fwd_ms, fwd_n = a.kernel_time()
+    with B.Algorithms(g.rowptr, g.colids, init=0) as a:
+        r0 = a.learnedLayout(np.zeros_like(params), sm, iterations, target, w["batch"], w["theta"], LR.STEP0)
+    flops = 2.0 * g.n * (32 * 64 + 2 * 128 * 64)
+    return {
+        "plain_energy": e_plain, "plain_s": plain_s,
+        "learned_s": r["seconds"], "learned_energy": r["energy"], "learned_iterations": r["iterations"],
+        "learned_start_s": r["init_seconds"], "fell_back": r["fell_back"],
+        "speedup": plain_s / r["seconds"] if r["seconds"] > 0 else None,
+        "mds_only_s": r0["seconds"], "mds_only_iterations": r0["iterations"], "mds_only_energy": r0["energy"],
+        "mpnn_forward_ms": fwd_ms, "mpnn_forward_tflops": flops / (fwd_ms * 1e-3) / 1e12 if fwd_ms > 0 else None,
+        "target": "plain run's final energy x 1.005",
+        "note": "wall seconds through the C ABI, starts included (greedy DFS on the host; features, network "
+                "and scale on the device); refinement STEP from 0.3; model batchlayoutcode_gb300/weights/"
+                "mpnn_bh.blw (48 graphs of 1k-100k vertices); mds_only = the same pipeline with a zero network",
+    }
+
+
 def run_reference_batched(args, w):
     """The reference lays out one graph per process: run its binary (else the
     port) graph by graph over the bounded sample with all host threads."""
@@ -451,6 +483,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="rgg1m", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()
@@ -561,6 +594,10 @@ def main():
                 "algorithmic_flops_per_launch": 10.0 * pairs,
                 "peak_source": "nominal FP32 FMA peak: 152 SMs x 128 lanes x 2 flops x max SM clock"}
 
+    tte = None
+    if algo == 4 and rank == 0 and not args.no_learned:
+        tte = time_to_energy(B, g, w)
+
     # end to end through the C ABI with pinned host buffers
     host_in = torch.empty((g.n, 2), dtype=torch.float64, pin_memory=True)
     host_out = torch.empty((g.n, 2), dtype=torch.float64, pin_memory=True)
@@ -589,6 +626,7 @@ def main():
                        "l2": "flushed before every timed step (256 MB write)",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+            "time_to_energy": tte,
         }
         print(json.dumps(line), flush=True)
     a.close()

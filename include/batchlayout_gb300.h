@@ -44,6 +44,7 @@ typedef struct bl_ctx bl_ctx;
  * (sample/algorithms.cpp:3-15).  Copies the CSR (rowptr[n+1], colids[nnz],
  * zero-based, as built by SetInputMatricesAsCSR, sample/commonutility.h:45-54)
  * to the device.  init: 0 greedy DFS, 1 random, 2 file (`initfile`).
+ * init 3 (an extension): the learned start, `initfile` naming the model file.
  * Returns NULL on failure (bl_create_error() then holds the reason). */
 bl_ctx *bl_algorithms_create(int device, int n, long long nnz, const int *rowptr,
                              const int *colids, const char *input,
@@ -260,6 +261,9 @@ int bl_learned_features(bl_ctx *ctx, int n, const int *rowptr, const int *colids
 int bl_learned_train(bl_ctx *ctx, int num_graphs, const int *vertex_offset, const long long *edge_offset,
                      const int *rowptr, const int *colids, const double *layouts, int epochs, double lr, int seed,
                      float *params, double *scale_model, double *loss_history);
+/* Read a model file (8 bytes "BLMPNN01", uint32 parameter count, the FP32
+ * parameters, the three FP64 scale-model coefficients, all little-endian). */
+int bl_learned_load_model(const char *path, float *params, double *scale_model);
 /* Replace the context's coordinates by the learned start for its graph (the
  * learned counterpart of bl_init_dfs): y + network output, scaled to the mean
  * edge length the scale model predicts. */
