@@ -51,7 +51,10 @@ WORKLOADS = {
                              "largest component; disc init; algo 2 (all-pairs minibatch), batch 256"),
     "grid64": dict(algo=2, batch=256, theta=1.2,
                    desc="64x64 triangulated grid (4,096 vertices, 12,033 edges); disc init; algo 2, batch 256"),
-    "batched2048": dict(algo="batched", batch=256, theta=1.2, iterations=300,
+    "batched256": dict(algo="batched", batch=256, theta=1.2, iterations=30, graphs=256,
+                       desc="profiling case of the batched launch: the first 256 graphs of the 2,048-graph mix "
+                            "(same generator and seed), 30 iterations"),
+    "batched2048": dict(algo="batched", batch=256, theta=1.2, iterations=300, graphs=2048,
                         desc="2,048 graphs, sizes log-uniform in 200-20,000 vertices, a third each of triangulated "
                              "grids, random geometric graphs (mean degree 6) and Chung-Lu graphs (exponent 2.5, "
                              "mean degree 8), disc init per graph; 300 iterations of algo 2 below 5,000 vertices "
@@ -165,8 +168,9 @@ def load_workload(name: str):
     return G.cached_workload(name)
 
 
-def load_batched(seed: int = 1):
-    """The 2,048-graph mix, cached as one .npz of concatenated arrays."""
+def load_batched(seed: int = 1, graphs: int = 2048):
+    """The 2,048-graph mix (its first `graphs` graphs), cached as one .npz of
+    concatenated arrays."""
     import numpy as np
     from batchlayoutcode_gb300 import graphs as G
     cache = os.path.join(ROOT, "batchlayoutcode_gb300", "_build", "workloads", f"batched2048_s{seed}.npz")
@@ -174,11 +178,11 @@ def load_batched(seed: int = 1):
         with np.load(cache) as z:
             vo, eo, rp, ci, xy, algo = (z[k] for k in ("vertex_offset", "edge_offset", "rowptr", "colids", "xy",
                                                        "algo"))
-        graphs = [(rp[vo[k] + k: vo[k + 1] + k + 1], ci[eo[k]:eo[k + 1]]) for k in range(vo.shape[0] - 1)]
-        xys = [xy[vo[k]:vo[k + 1]] for k in range(vo.shape[0] - 1)]
-        return graphs, xys, algo
+        count = min(graphs, vo.shape[0] - 1)
+        gl = [(rp[vo[k] + k: vo[k + 1] + k + 1], ci[eo[k]:eo[k + 1]]) for k in range(count)]
+        xys = [xy[vo[k]:vo[k + 1]] for k in range(count)]
+        return gl, xys, algo[:count]
     gs, xys, algo = G.batched_mix(2048, 200, 20000, seed)
-    graphs = [(g.rowptr, g.colids) for g in gs]
     vo = np.zeros(len(gs) + 1, np.int64)
     vo[1:] = np.cumsum([g.n for g in gs])
     eo = np.zeros(len(gs) + 1, np.int64)
@@ -186,7 +190,7 @@ def load_batched(seed: int = 1):
     os.makedirs(os.path.dirname(cache), exist_ok=True)
     np.savez(cache, vertex_offset=vo, edge_offset=eo, rowptr=np.concatenate([g.rowptr for g in gs]),
              colids=np.concatenate([g.colids for g in gs]), xy=np.concatenate(xys), algo=algo)
-    return graphs, xys, algo
+    return [(g.rowptr, g.colids) for g in gs[:graphs]], xys[:graphs], algo[:graphs]
 
 
 def batched_sample(graphs, algo, iterations):
@@ -307,7 +311,7 @@ def time_to_energy(B, g, w, iterations: int = 600):
 def run_reference_batched(args, w):
     """The reference lays out one graph per process: run its binary (else the
     port) graph by graph over the bounded sample with all host threads."""
-    graphs, xys, algo = load_batched()
+    graphs, xys, algo = load_batched(graphs=w["graphs"])
     cores = os.cpu_count() or 1
     pick, it = batched_sample(graphs, algo, w["iterations"])
     ref_bin = os.path.join(ROOT, "oracle", "_ref", "BatchLayout")
@@ -365,7 +369,7 @@ def run_batched(args, w, ws, rank, local):
     device = local if ws > 1 else 0
     import batchlayoutcode_gb300 as B
     B.build()
-    graphs, xys, algo = load_batched()
+    graphs, xys, algo = load_batched(graphs=w["graphs"])
     iters, batch, theta = w["iterations"], w["batch"], w["theta"]
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
