@@ -52,17 +52,24 @@ __device__ __forceinline__ void dev_record_error(DevStatus *st, unsigned int cod
   if (atomicCAS(&st->code, 0u, code) == 0u) st->where = blockIdx.x;
 }
 
-// Grid-wide barrier for a cooperative (co-resident) launch.  `epoch` counts
-// the barriers this block has passed; the counter is monotone within one
-// launch and reset by the host before it.  Returns false when the grid must
-// stop (timeout here or an error recorded elsewhere).
-__device__ __forceinline__ bool grid_barrier(DevStatus *st, unsigned int &epoch) {
+// Grid-wide barrier for a cooperative (co-resident) launch, in two halves so
+// that a block can do independent work between announcing its arrival and
+// waiting for the others.  `epoch` counts the barriers this block has passed;
+// the counter is monotone within one launch and reset by the host before it.
+// grid_wait returns false when the grid must stop (timeout here or an error
+// recorded elsewhere).
+__device__ __forceinline__ void grid_arrive(DevStatus *st, unsigned int &epoch) {
   __syncthreads();
   epoch++;
-  __shared__ unsigned int s_ok;
   if (threadIdx.x == 0) {
     __threadfence();
     atomicAdd(&st->barrier, 1u);
+  }
+}
+
+__device__ __forceinline__ bool grid_wait(DevStatus *st, unsigned int epoch) {
+  __shared__ unsigned int s_ok;
+  if (threadIdx.x == 0) {
     const unsigned int target = epoch * gridDim.x;
     const unsigned long long t0 = dev_globaltimer();
     unsigned int ok = 1, polls = 0;
@@ -84,6 +91,11 @@ __device__ __forceinline__ bool grid_barrier(DevStatus *st, unsigned int &epoch)
   }
   __syncthreads();
   return s_ok != 0;
+}
+
+__device__ __forceinline__ bool grid_barrier(DevStatus *st, unsigned int &epoch) {
+  grid_arrive(st, epoch);
+  return grid_wait(st, epoch);
 }
 
 __device__ __forceinline__ float rcp_approx(float x) {

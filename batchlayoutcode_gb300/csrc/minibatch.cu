@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
   const int tid = threadIdx.x;
   const int grp = tid / kGroup, gl = tid % kGroup;
 
-  for (int k = tid; k < slen; k += kThreads) slice[k] = a.pos[sbase + k];
+  for (int k = tid; k < slen; k += kThreads) slice[k] = __ldcg(&a.pos[sbase + k]);
   // group sub-ranges of [slo, shi) in slice-local indices
   const int la = slo - sbase, lb = shi - sbase;
   const int ga = la + (int)((long long)(lb - la) * grp / kGroups);
@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
       // the first batch of the run, and every batch when there is only one,
       // loads them here
       if (!prefetched) {
-        for (int t = tid; t < cnt; t += kThreads) tpos[t] = a.pos[base + t];
+        for (int t = tid; t < cnt; t += kThreads) tpos[t] = __ldcg(&a.pos[base + t]);
         if (cnt <= kChunk) stage_neighbours(a, nblist(buf), s, base, cnt, slo, shi, sbase);
       }
       __syncthreads();
@@ -337,8 +337,11 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
         }
         __syncthreads();
       }
-      // prefetch the next batch's targets and cursors: its vertices do not
-      // move before it, and the cursors depend on the graph only
+      // announce this block's partials, then prefetch the next batch's targets
+      // and cursors while the other blocks arrive: its vertices do not move
+      // before it, and the cursors depend on the graph only.  Positions are
+      // read through L2: other blocks moved them.
+      grid_arrive(a.st, epoch);
       {
         const int cn = (c + 1 < a.nbatches) ? c + 1 : 0;
         prefetched = (cn != c);  // a single batch moves itself: reload after the update
@@ -346,11 +349,11 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
           const int nbase = cn * a.batch;
           const int ncnt = min(a.batch, a.n - nbase);
           float2 *ntpos = tbuf + (int)((seq + 1u) & 1u) * a.batch;
-          for (int t = tid; t < ncnt; t += kThreads) ntpos[t] = a.pos[nbase + t];
+          for (int t = tid; t < ncnt; t += kThreads) ntpos[t] = __ldcg(&a.pos[nbase + t]);
           if (ncnt <= kChunk) stage_neighbours(a, nblist((seq + 1u) & 1u), s, nbase, ncnt, slo, shi, sbase);
         }
       }
-      ok = grid_barrier(a.st, epoch);
+      ok = grid_wait(a.st, epoch);
       if (!ok) break;
       // ---- owners: read the summed force, update, clear the accumulator -----
       const int olo = max(slo, base), ohi = min(shi, base + cnt);
