@@ -388,7 +388,7 @@ __global__ void __launch_bounds__(256) level_fill_kernel(TreeArgs t) {
 // levels: the unweighted mean of the children summed in quadrant order in
 // FP64 (BarnesHut.h:197-217), bit-identical to the reference.
 __global__ void __launch_bounds__(1024) centroid_kernel(TreeArgs t) {
-  if (ld_volatile_u32(&t.st->code) != 0u) return;
+  if (!block_status_ok(t.st)) return;
   unsigned int epoch = 0;
   const int gsz = gridDim.x * blockDim.x;
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -461,7 +461,7 @@ struct LayoutArgs {
 
 __global__ void layout_kernel(LayoutArgs L, TreeArgs t) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ld_volatile_u32(&L.st->code) != 0u) return;
+  if (!block_status_ok(L.st)) return;
   const double maxmin = L.frame[2];
   const int cap = 2 * L.n - 1;  // records: n leaves + at most n-1 quad nodes
   if (i < L.n) {  // leaf (sorted point) i
@@ -521,8 +521,8 @@ struct TraverseArgs {
 
 __global__ void __launch_bounds__(256) traverse_kernel(TraverseArgs a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!block_status_ok(a.st)) return;  // the tree of this iteration is not valid
   if (k >= a.n) return;
-  if (ld_volatile_u32(&a.st->code) != 0u) return;  // the tree of this iteration is not valid
   const float2 q = a.spos[k];
   // record 0 is the root; its skip link is the number of records
   int total = __float_as_int(__ldg(&a.nodes[0]).w);
@@ -585,7 +585,7 @@ __device__ __forceinline__ void sweep_vertex(const SweepArgs &a, int t) {
 // One cooperative launch for all dependency levels of an iteration; a
 // bounded grid barrier separates the levels.
 __global__ void __launch_bounds__(kSweepThreads, 2) sweep_kernel(SweepArgs a) {
-  if (ld_volatile_u32(&a.st->code) != 0u) return;  // every block sees the same value: no barrier is left waiting
+  if (!block_status_ok(a.st)) return;  // every block sees the same value: no barrier is left waiting
   unsigned int epoch = 0;
   const int gsz = gridDim.x * blockDim.x;
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x;

@@ -48,6 +48,16 @@ __device__ __forceinline__ unsigned int ld_volatile_u32(const unsigned int *p) {
   return *reinterpret_cast<const volatile unsigned int *>(p);
 }
 
+// Whether no earlier launch recorded an error: one read per block, shared
+// (every thread reading the same word would queue at one L2 slice).  All
+// threads of the block must call it, before any early return.
+__device__ __forceinline__ bool block_status_ok(const DevStatus *st) {
+  __shared__ unsigned int s_code;
+  if (threadIdx.x == 0) s_code = ld_volatile_u32(&st->code);
+  __syncthreads();
+  return s_code == 0u;
+}
+
 __device__ __forceinline__ void dev_record_error(DevStatus *st, unsigned int code) {
   if (atomicCAS(&st->code, 0u, code) == 0u) st->where = blockIdx.x;
 }

@@ -11,9 +11,13 @@
 //   f[14]     mean of log2(1 + deg) over the neighbours,
 //   f[15]     log2(n) / 20.
 // Hop distances come from one multi-source BFS on the device (a 16-bit
-// visited mask per vertex, one level per grid-barrier step, pull from the
-// neighbours' frontier masks); all graphs of a training set run in the same
-// BFS, each with its own pivots.  Distances to pivots that a vertex cannot
+// visited mask per vertex, one level per grid-barrier step, the vertices of
+// the level's frontier push their new source bits to their neighbours, which
+// join the next frontier list the first time a bit reaches them); all graphs
+// of a training set run in the same BFS, each with its own pivots.  The work
+// of a level is its frontier (the 1M-vertex random geometric graph has 1,430
+// levels), and a block gathers its new frontier vertices in shared memory and
+// reserves room for them in the global list with one atomic per level.  Distances to pivots that a vertex cannot
 // reach count as one more than the pivot's largest finite distance.
 #include <algorithm>
 #include <cmath>
@@ -29,81 +33,100 @@ namespace bl {
 namespace {
 
 constexpr int kP = kPivots;
-constexpr unsigned int kAll = (1u << kP) - 1u;
 constexpr unsigned short kUnreached = 0xFFFF;
 
-__global__ void bfs_init_kernel(int n, unsigned int *visited, unsigned int *fr0, unsigned short *dist) {
+__global__ void bfs_init_kernel(int n, unsigned int *visited, unsigned int *fr0, unsigned int *fr1,
+                                unsigned short *dist) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   visited[v] = 0u;
   fr0[v] = 0u;
+  fr1[v] = 0u;
 #pragma unroll
   for (int s = 0; s < kP; s++) dist[(size_t)v * kP + s] = kUnreached;
 }
 
-// pivots[g * 16 + s]: global vertex of pivot s of graph g
+// pivots[g * 16 + s]: global vertex of pivot s of graph g; the distinct pivot
+// vertices form the frontier list of level 0
 __global__ void bfs_seed_kernel(int count, const int *pivots, unsigned int *visited, unsigned int *fr0,
-                                unsigned short *dist) {
+                                unsigned short *dist, int *wl0, unsigned int *cnt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   const int p = pivots[i], s = i % kP;
   atomicOr(&visited[p], 1u << s);
-  atomicOr(&fr0[p], 1u << s);
   dist[(size_t)p * kP + s] = 0;
+  if (atomicOr(&fr0[p], 1u << s) == 0u) wl0[atomicAdd(&cnt[0], 1u)] = p;
 }
 
 struct BfsArgs {
   int n;
   const int *rowptr, *colids;
-  unsigned int *visited, *fr0, *fr1;
+  unsigned int *visited;
+  unsigned int *fr[2];   // frontier masks: bits that reached the vertex at the level
+  int *wl[2];            // frontier lists
+  unsigned int *cnt;     // [3] list lengths, rotating by level
   unsigned short *dist;
-  unsigned int *progress;
   DevStatus *st;
   int max_levels;
 };
 
-// One cooperative launch; level L pulls the frontier of level L-1 from the
-// neighbours.  A vertex is always handled by the same thread, so visited[]
-// needs no atomics; frontier masks written by other blocks are read through
-// L2 (__ldcg) after the grid barrier.  Stops after a level without news.
+constexpr int kBfsBuf = 2048;  // new frontier vertices a block gathers per level before spilling
+
+// One cooperative launch, one level per bounded grid barrier.  Level L reads
+// the list of level L-1 (fr[(L-1)&1], wl[(L-1)&1], cnt[(L-1)%3]) and builds
+// the list of level L; a frontier vertex's mask is cleared once pushed, so a
+// mask buffer holds only its own list's vertices.  Lists and masks written by
+// other blocks are read through L2 (__ldcg) after the barrier.
 __global__ void __launch_bounds__(512) msbfs_kernel(BfsArgs a) {
-  __shared__ int s_found;
-  unsigned int epoch = 0, prev = 0;
-  const int gsz = gridDim.x * blockDim.x, t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ unsigned int s_count, s_n, s_base;
+  __shared__ int s_buf[kBfsBuf];
+  unsigned int epoch = 0;
+  const unsigned int lane = threadIdx.x & 31u;
+  const unsigned int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const unsigned int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int L = 1; L <= a.max_levels; L++) {
-    const unsigned int *cur = (L & 1) ? a.fr0 : a.fr1;
-    unsigned int *nxt = (L & 1) ? a.fr1 : a.fr0;
-    if (threadIdx.x == 0) s_found = 0;
+    const int cb = (L - 1) & 1, nbuf = L & 1;
+    // one read per block; all appends preceded the barrier, so every block
+    // sees the same value
+    if (threadIdx.x == 0) {
+      s_count = ld_acquire_gpu(&a.cnt[(L - 1) % 3]);
+      s_n = 0u;
+    }
     __syncthreads();
-    bool found = false;
-    for (int v = t0; v < a.n; v += gsz) {
-      const unsigned int vis = a.visited[v];
-      unsigned int nw = 0u;
-      if (vis != kAll) {
-        unsigned int m = 0u;
-        const int e1 = a.rowptr[v + 1];
-        for (int e = a.rowptr[v]; e < e1; e++) m |= __ldcg(&cur[a.colids[e]]);
-        nw = m & ~vis & kAll;
-        if (nw) {
-          a.visited[v] = vis | nw;
-          unsigned int b = nw;
-          while (b) {
-            const int s = __ffs(b) - 1;
-            b &= b - 1u;
-            a.dist[(size_t)v * kP + s] = (unsigned short)min(L, 65534);
-          }
-          found = true;
+    const unsigned int count = s_count;
+    if (count == 0u) break;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.cnt[(L + 1) % 3] = 0u;  // untouched during this level
+    // a warp per frontier vertex, a lane per neighbour: a level costs one
+    // neighbour's chain of dependent L2 round trips, not deg of them
+    for (unsigned int idx = wid; idx < count; idx += nwarps) {
+      const int u = __ldcg(&a.wl[cb][idx]);
+      const unsigned int m = __ldcg(&a.fr[cb][u]);
+      const int e0 = a.rowptr[u], e1 = a.rowptr[u + 1];
+      __syncwarp();
+      if (lane == 0) a.fr[cb][u] = 0u;
+      for (int e = e0 + lane; e < e1; e += 32) {
+        const int v = a.colids[e];
+        const unsigned int got = m & ~atomicOr(&a.visited[v], m);
+        if (!got) continue;
+        unsigned int b = got;
+        while (b) {
+          const int s = __ffs(b) - 1;
+          b &= b - 1u;
+          a.dist[(size_t)v * kP + s] = (unsigned short)min(L, 65534);
+        }
+        if (atomicOr(&a.fr[nbuf][v], got) == 0u) {
+          const unsigned int slot = atomicAdd(&s_n, 1u);
+          if (slot < (unsigned int)kBfsBuf) s_buf[slot] = v;
+          else a.wl[nbuf][atomicAdd(&a.cnt[L % 3], 1u)] = v;  // rare spill
         }
       }
-      nxt[v] = nw;
     }
-    if (found) s_found = 1;
     __syncthreads();
-    if (threadIdx.x == 0 && s_found) atomicAdd(a.progress, 1u);
+    const unsigned int mine = min(s_n, (unsigned int)kBfsBuf);
+    if (threadIdx.x == 0 && mine) s_base = atomicAdd(&a.cnt[L % 3], mine);
+    __syncthreads();
+    for (unsigned int k = threadIdx.x; k < mine; k += blockDim.x) a.wl[nbuf][s_base + k] = s_buf[k];
     if (!grid_barrier(a.st, epoch)) return;
-    const unsigned int p = ld_acquire_gpu(a.progress);
-    if (p == prev) break;
-    prev = p;
   }
 }
 
@@ -339,13 +362,14 @@ int compute_features(bl_ctx *ctx, int num_graphs, const int *voff, int n, const 
                      const int *pivots, float *d_features, unsigned short *d_dist) {
   cudaStream_t st = ctx->stream;
   const int P = num_graphs * kP;
-  unsigned int *visited = nullptr, *fr0 = nullptr, *fr1 = nullptr, *progress = nullptr;
-  int *d_piv = nullptr, *d_maxd = nullptr, *d_ipart = nullptr;
+  unsigned int *visited = nullptr, *fr0 = nullptr, *fr1 = nullptr, *cnt = nullptr;
+  int *d_piv = nullptr, *d_maxd = nullptr, *d_ipart = nullptr, *wl0 = nullptr, *wl1 = nullptr;
   double *d_dpart = nullptr, *d_colmean = nullptr, *d_V = nullptr;
   const int kBlocks = 256;
   int rc = 0;
   auto cleanup = [&]() {
-    cudaFree(visited); cudaFree(fr0); cudaFree(fr1); cudaFree(progress); cudaFree(d_piv); cudaFree(d_maxd);
+    cudaFree(visited); cudaFree(fr0); cudaFree(fr1); cudaFree(cnt); cudaFree(wl0); cudaFree(wl1);
+    cudaFree(d_piv); cudaFree(d_maxd);
     cudaFree(d_ipart); cudaFree(d_dpart); cudaFree(d_colmean); cudaFree(d_V);
   };
   auto ck = [&](cudaError_t e, const char *w) {
@@ -355,7 +379,9 @@ int compute_features(bl_ctx *ctx, int num_graphs, const int *voff, int n, const 
   ck(cudaMalloc(&visited, sizeof(unsigned int) * n), "cudaMalloc");
   ck(cudaMalloc(&fr0, sizeof(unsigned int) * n), "cudaMalloc");
   ck(cudaMalloc(&fr1, sizeof(unsigned int) * n), "cudaMalloc");
-  ck(cudaMalloc(&progress, sizeof(unsigned int)), "cudaMalloc");
+  ck(cudaMalloc(&cnt, 3 * sizeof(unsigned int)), "cudaMalloc");
+  ck(cudaMalloc(&wl0, sizeof(int) * n), "cudaMalloc");
+  ck(cudaMalloc(&wl1, sizeof(int) * n), "cudaMalloc");
   ck(cudaMalloc(&d_piv, sizeof(int) * P), "cudaMalloc");
   ck(cudaMalloc(&d_maxd, sizeof(int) * kP), "cudaMalloc");
   ck(cudaMalloc(&d_ipart, sizeof(int) * kBlocks * kP), "cudaMalloc");
@@ -367,21 +393,23 @@ int compute_features(bl_ctx *ctx, int num_graphs, const int *voff, int n, const 
     return rc;
   }
   ck(cudaMemcpyAsync(d_piv, pivots, sizeof(int) * P, cudaMemcpyHostToDevice, st), "H2D");
-  bfs_init_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, visited, fr0, d_dist);
-  bfs_seed_kernel<<<(P + 255) / 256, 256, 0, st>>>(P, d_piv, visited, fr0, d_dist);
-  ck(cudaMemsetAsync(progress, 0, sizeof(unsigned int), st), "memset");
+  ck(cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned int), st), "memset");
+  bfs_init_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, visited, fr0, fr1, d_dist);
+  bfs_seed_kernel<<<(P + 255) / 256, 256, 0, st>>>(P, d_piv, visited, fr0, d_dist, wl0, cnt);
   ck(cudaMemsetAsync(&ctx->s.status->barrier, 0, sizeof(unsigned int), st), "memset");
   ctx->launches += 2;
   {
     int occ = 0;
     ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, msbfs_kernel, 512, 0), "occupancy");
     if (!rc && occ < 1) rc = bl_fail(ctx, BL_ERR_TOO_LARGE, "BFS kernel cannot be resident");
-    BfsArgs b{n, d_rowptr, d_colids, visited, fr0, fr1, d_dist, progress, ctx->s.status, n + 1};
+    BfsArgs b{n, d_rowptr, d_colids, visited, {fr0, fr1}, {wl0, wl1}, cnt, d_dist, ctx->s.status, n + 1};
     void *args[] = {&b};
+    bl_time_begin(ctx, "msbfs_kernel");
     if (!rc)
       ck(cudaLaunchCooperativeKernel((const void *)msbfs_kernel, dim3(ctx->num_sms * std::min(occ, 2)), dim3(512),
                                      args, 0, st),
          "BFS launch");
+    bl_time_end(ctx, "msbfs_kernel");
     ctx->launches++;
   }
   if (!rc) ck(cudaStreamSynchronize(st), "BFS");
