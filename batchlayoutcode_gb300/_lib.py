@@ -315,10 +315,13 @@ class Algorithms:
         return out, (int(st[0]), int(st[1]))
 
     def run_resident(self, algo: int, iterations: int, batch: int = 256, theta: float = 1.2,
-                     step: float = 1.0) -> float:
+                     step: float = 1.0, want_energy: bool = True):
+        """Device-resident iterations; the last iteration's energy (None when
+        want_energy is False, algo 4 only: then no energy is computed)."""
         e = C.c_double()
-        self._check(self._L.bl_run_resident(self._ctx, algo, iterations, batch, theta, step, C.byref(e)))
-        return e.value
+        self._check(self._L.bl_run_resident(self._ctx, algo, iterations, batch, theta, step,
+                                            C.byref(e) if want_energy else None))
+        return e.value if want_energy else None
 
     def last_run_ms(self) -> float:
         """CUDA-event device time of the last run_resident call."""

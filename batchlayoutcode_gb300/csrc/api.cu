@@ -142,6 +142,8 @@ void free_ctx(bl_ctx *c) {
   c->batched = nullptr;
   bl::mpnn_free(c->mpnn);
   c->mpnn = nullptr;
+  bl::bh_graph_free(c->bh_graph);
+  c->bh_graph = nullptr;
   for (auto ev : c->ev_pool) cudaEventDestroy(ev);
   for (auto ev : c->run_ev)
     if (ev) cudaEventDestroy(ev);
@@ -583,8 +585,18 @@ int bl_run_resident(bl_ctx *ctx, int algo, int iterations, int batch, double the
   } else if (algo == 4) {
     if (batch < 1) return bl_fail(ctx, BL_ERR_ARG, "batch must be >= 1");
     double s = step;
-    for (int it = 0; it < iterations && rc == 0; it++) {
-      const bool last = it == iterations - 1;
+    int it = 0;
+    const bool want_energy = energy_out != nullptr;
+    const int replay = want_energy ? iterations - 1 : iterations;
+    if (ctx->graph_mode && replay > 0) {
+      // iterations without energy read-back replay the captured iteration;
+      // if it cannot be captured, they are launched directly
+      const int r = bl::bh_graph_iterations(ctx, batch, theta, &s, replay);
+      if (r < 0) return r;
+      if (r == 0) it = replay;
+    }
+    for (; it < iterations && rc == 0; it++) {
+      const bool last = want_energy && it == iterations - 1;
       rc = bl::bh_iteration(ctx, batch, theta, s, last, last ? &energy : nullptr);
       s = s * 0.999;
     }
@@ -599,6 +611,7 @@ int bl_run_resident(bl_ctx *ctx, int algo, int iterations, int batch, double the
   ctx->last_run_ms = ms;
   collect_timing(ctx);
   if (energy_out) *energy_out = energy;
+  if (algo == 4 && !energy_out) return bl_check_status(ctx);
   return BL_OK;
 }
 

@@ -796,6 +796,132 @@ int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_en
   return 0;
 }
 
+// ---- CUDA-graph replay of the iteration ------------------------------------
+// One Barnes-Hut iteration without the energy read-back is a fixed sequence
+// of about 45 launches and memsets on fixed buffers; only the positions
+// alternate between two buffers and STEP changes.  It is captured once per
+// parity of the position buffers and replayed, STEP being set on the sweep's
+// kernel node before each replay.
+struct BhGraph {
+  int batch = -1;
+  double theta = 0.0;
+  float2 *pos0 = nullptr;  // ctx->pos of the parity-0 graph
+  cudaGraph_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  cudaGraphNode_t sweep[2] = {nullptr, nullptr};
+  SweepArgs args[2];
+  cudaKernelNodeParams params[2];
+  long long kernels[2] = {0, 0};
+};
+
+void bh_graph_free(BhGraph *g) {
+  if (!g) return;
+  for (int p = 0; p < 2; p++) {
+    if (g->exec[p]) cudaGraphExecDestroy(g->exec[p]);
+    if (g->graph[p]) cudaGraphDestroy(g->graph[p]);
+  }
+  delete g;
+}
+
+namespace {
+
+// Capture parity p (positions read from ctx->pos, written to s.pos_alt).
+// Returns 0, or 1 when the iteration cannot be captured (nothing has run).
+int bh_graph_capture(bl_ctx *ctx, BhGraph &G, int p, int batch, double theta) {
+  float2 *save_pos = ctx->pos, *save_alt = ctx->s.pos_alt;
+  const std::string save_timed = ctx->timed_kernel;
+  const long long save_launches = ctx->launches;
+  ctx->timed_kernel.clear();  // no timing events inside the graph
+  if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->timed_kernel = save_timed;
+    return 1;
+  }
+  const int rc = bh_iteration(ctx, batch, theta, 1.0, false, nullptr);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+  ctx->pos = save_pos;
+  ctx->s.pos_alt = save_alt;
+  ctx->timed_kernel = save_timed;
+  G.kernels[p] = ctx->launches - save_launches;
+  ctx->launches = save_launches;
+  if (rc || e != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return 1;
+  }
+  size_t count = 0;
+  cudaGraphGetNodes(graph, nullptr, &count);
+  std::vector<cudaGraphNode_t> nodes(count);
+  cudaGraphGetNodes(graph, nodes.data(), &count);
+  cudaGraphNode_t sweep = nullptr;
+  for (cudaGraphNode_t nd : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+    cudaKernelNodeParams kp;
+    if (cudaGraphKernelNodeGetParams(nd, &kp) != cudaSuccess) continue;
+    if (kp.func == (void *)sweep_kernel) {
+      sweep = nd;
+      G.params[p] = kp;
+      G.args[p] = *static_cast<SweepArgs *>(kp.kernelParams[0]);
+    }
+  }
+  cudaGraphExec_t exec = nullptr;
+  if (!sweep || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return 1;
+  }
+  G.graph[p] = graph;
+  G.exec[p] = exec;
+  G.sweep[p] = sweep;
+  return 0;
+}
+
+}  // namespace
+
+// `count` iterations without energy read-back by graph replay, STEP from
+// *step (multiplied by 0.999 after each).  Returns 0, an error code, or 1
+// when the iteration cannot be captured (nothing has run; launch directly).
+int bh_graph_iterations(bl_ctx *ctx, int batch, double theta, double *step, int count) {
+  if (count <= 0) return 0;
+  if (int rc = ensure_bh_scratch(ctx)) return rc;
+  if (!level_schedule(ctx, batch)) return -2;
+  BhGraph *G = ctx->bh_graph;
+  const bool fresh = !G || G->batch != batch || G->theta != theta ||
+                     (G->pos0 != ctx->pos && G->pos0 != ctx->s.pos_alt);
+  if (fresh) {
+    bh_graph_free(G);
+    G = ctx->bh_graph = new BhGraph();
+    G->batch = batch;
+    G->theta = theta;
+    G->pos0 = ctx->pos;
+    // parity 1 reads the other buffer
+    std::swap(ctx->pos, ctx->s.pos_alt);
+    const int r1 = bh_graph_capture(ctx, *G, 1, batch, theta);
+    std::swap(ctx->pos, ctx->s.pos_alt);
+    const int r0 = r1 ? 1 : bh_graph_capture(ctx, *G, 0, batch, theta);
+    if (r0 || r1) {
+      bh_graph_free(G);
+      ctx->bh_graph = nullptr;
+      return 1;
+    }
+  }
+  for (int k = 0; k < count; k++) {
+    const int p = (ctx->pos == G->pos0) ? 0 : 1;
+    G->args[p].step = (float)*step;
+    void *kargs[] = {&G->args[p]};
+    cudaKernelNodeParams kp = G->params[p];
+    kp.kernelParams = kargs;
+    BL_CUDA(ctx, cudaGraphExecKernelNodeSetParams(G->exec[p], G->sweep[p], &kp));
+    BL_CUDA(ctx, cudaGraphLaunch(G->exec[p], ctx->stream));
+    ctx->launches += G->kernels[p];
+    std::swap(ctx->pos, ctx->s.pos_alt);
+    *step *= 0.999;
+  }
+  return 0;
+}
+
 int bh_canonical_tree(bl_ctx *ctx, int cap, int *lo, int *hi, int *depth, int *nchild,
                       double *centroid) {
   const int n = ctx->g.n;

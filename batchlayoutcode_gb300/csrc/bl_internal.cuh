@@ -201,6 +201,7 @@ struct Scratch {
 namespace bl {
 struct BatchedState;
 struct MpnnState;
+struct BhGraph;
 }
 
 struct bl_ctx {
@@ -234,6 +235,7 @@ struct bl_ctx {
   double last_run_ms = 0.0;
   bl::BatchedState *batched = nullptr;  // many-graph layout (batched.cu)
   bl::MpnnState *mpnn = nullptr;        // learned initializer (mpnn.cu)
+  bl::BhGraph *bh_graph = nullptr;      // captured Barnes-Hut iteration (barnes_hut.cu)
 };
 
 // ---- helpers implemented in api.cu ---------------------------------------
@@ -268,6 +270,8 @@ void cursor_neighbours(int n, const std::vector<int> &rp, const std::vector<int>
 struct BatchedState;
 void batched_free(BatchedState *b);
 void mpnn_free(MpnnState *m);
+void bh_graph_free(BhGraph *g);
+int bh_graph_iterations(bl_ctx *ctx, int batch, double theta, double *step, int count);
 int energy_reduce(bl_ctx *ctx, double *out_host);
 int scan_exclusive_int(bl_ctx *ctx, const int *in, int *out, int n);
 }  // namespace bl

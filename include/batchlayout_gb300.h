@@ -150,14 +150,19 @@ int bl_bh_repulsion(bl_ctx *ctx, double theta, double *out, long long *stats);
 /* Device-resident run for throughput measurement: `iterations` iterations of
  * algo (2, 3, 4 or 8) from the current device coordinates, no init, no host
  * copies; STEP starts at `step` and decays as in the reference.
- * energy_out = energy of the last iteration. */
+ * energy_out = energy of the last iteration; for algo 4 it may be NULL, and
+ * then no energy is computed. */
 int bl_run_resident(bl_ctx *ctx, int algo, int iterations, int batch, double theta,
                     double step, double *energy_out);
 /* Device time of the last bl_run_resident call: CUDA events recorded on the
  * context's stream before its first and after its last kernel. */
 int bl_last_run_ms(bl_ctx *ctx, double *ms);
-/* Make the next bl_run_resident calls (same algo, batch, theta) replay a
- * captured CUDA graph of one iteration (1) or launch kernels directly (0). */
+/* Make bl_run_resident with algo 4 replay a captured CUDA graph of one
+ * iteration for all iterations but the last (1), or launch every kernel
+ * directly (0, the default).  The graph is captured on first use for the
+ * given batch and theta and kept until they change; the results are the same
+ * bits either way.  If the iteration cannot be captured the kernels are
+ * launched directly. */
 int bl_set_graph_mode(bl_ctx *ctx, int enabled);
 /* CUDA events around the dominant kernel of the last bl_run_resident call:
  * ms[0] = total milliseconds of that kernel, ms[1] = number of launches. */

@@ -352,3 +352,21 @@ def test_multi_iteration_launch_equals_single_iterations(B, model):
             step *= decay
         single = a.nCoordinates
     assert np.array_equal(multi, single)
+
+
+def test_graph_mode_replays_the_same_iterations(B):
+    """bl_set_graph_mode(1): all but the last iteration of a resident
+    Barnes-Hut run replay a captured CUDA graph; the bits are the same."""
+    from batchlayoutcode_gb300 import graphs as G
+    g = G.random_geometric(20_000, 6.0, seed=5)
+    xy = G.init_square(g.n, seed=5)
+    out = {}
+    for mode in (False, True):
+        with B.Algorithms(g.rowptr, g.colids) as a:
+            a.nCoordinates = xy
+            a.set_graph_mode(mode)
+            e1 = a.run_resident(4, 7, 256, 1.2, 1.0)
+            e2 = a.run_resident(4, 6, 256, 1.2, 0.999 ** 7)  # replays the cached graphs
+            out[mode] = (e1, e2, a.nCoordinates)
+    assert out[True][0] == out[False][0] and out[True][1] == out[False][1]
+    assert np.array_equal(out[True][2], out[False][2])
