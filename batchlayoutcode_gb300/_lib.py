@@ -27,7 +27,8 @@ EXPORTS = (
     "bl_batched_result", "bl_batched_layout", "bl_batched_parts", "bl_batched_set_parts",
     "bl_batched_graph_cycles", "bl_mpnn_set_params", "bl_mpnn_get_params", "bl_mpnn_run",
     "bl_learned_features", "bl_learned_train", "bl_learned_init", "bl_learned_layout",
-    "bl_learned_load_model",
+    "bl_learned_load_model", "bl_approx_force_directed", "bl_cache_blocking_minibatch_sd",
+    "bl_greedy_iteration", "bl_greedy_walks",
 )
 
 _lib = None
@@ -105,6 +106,10 @@ def load() -> C.CDLL:
         "bl_learned_init": (i32, [vp, C.POINTER(C.c_float), dp, i32]),
         "bl_learned_layout": (i32, [vp, C.POINTER(C.c_float), dp, i32, i32, i32, f64, f64, f64, dp]),
         "bl_learned_load_model": (i32, [cp, C.POINTER(C.c_float), dp]),
+        "bl_approx_force_directed": (i32, [vp, i32, i32, i32, dp]),
+        "bl_cache_blocking_minibatch_sd": (i32, [vp, i32, i32, i32, i32, dp]),
+        "bl_greedy_iteration": (i32, [vp, i32, f64, dp]),
+        "bl_greedy_walks": (i32, [vp, C.POINTER(C.c_longlong), ip, ip, i64, C.POINTER(C.c_longlong)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -275,6 +280,16 @@ class Algorithms:
         self._check(self._L.bl_approx_cache_block_bh(self._ctx, ITERATIONS, NUMOFTHREADS, BATCHSIZE, o))
         return [o[0], o[1]]
 
+    def approxForceDirectedAlgorithm(self, ITERATIONS, NUMOFTHREADS=0, BATCHSIZE=256):
+        o = self._out()
+        self._check(self._L.bl_approx_force_directed(self._ctx, ITERATIONS, NUMOFTHREADS, BATCHSIZE, o))
+        return [o[0], o[1]]
+
+    def cacheBlockingminiBatchForceDirectedAlgorithmSD(self, ITERATIONS, NUMOFTHREADS=0, BATCHSIZE=256, flag=0):
+        o = self._out()
+        self._check(self._L.bl_cache_blocking_minibatch_sd(self._ctx, ITERATIONS, NUMOFTHREADS, BATCHSIZE, flag, o))
+        return [o[0], o[1]]
+
     def writeToFile(self, f: str) -> str:
         buf = C.create_string_buffer(4096)
         self._check(self._L.bl_write_to_file(self._ctx, f.encode(), buf, 4096))
@@ -285,6 +300,24 @@ class Algorithms:
         e = C.c_double()
         self._check(self._L.bl_minibatch_iteration(self._ctx, model, batch, step, C.byref(e)))
         return e.value
+
+    def greedy_iteration(self, batch: int, step: float) -> float:
+        """One first-phase iteration of algo 5."""
+        e = C.c_double()
+        self._check(self._L.bl_greedy_iteration(self._ctx, batch, step, C.byref(e)))
+        return e.value
+
+    def greedy_walks(self):
+        """Algo 5's walk sources -> (offsets int64 [n+1], sources int32, counts int32)."""
+        off = np.zeros(self.n + 1, np.int64)
+        total = C.c_longlong()
+        llp = C.POINTER(C.c_longlong)
+        self._check(self._L.bl_greedy_walks(self._ctx, off.ctypes.data_as(llp), None, None, 0, C.byref(total)))
+        src = np.zeros(max(total.value, 1), np.int32)
+        cnt = np.zeros(max(total.value, 1), np.int32)
+        self._check(self._L.bl_greedy_walks(self._ctx, off.ctypes.data_as(llp), _ip(src), _ip(cnt), total.value,
+                                            C.byref(total)))
+        return off, src[:total.value], cnt[:total.value]
 
     def barnes_hut_iteration(self, batch: int, theta: float, step: float) -> float:
         e = C.c_double()

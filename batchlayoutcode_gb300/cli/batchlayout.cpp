@@ -142,8 +142,8 @@ int main(int argc, char *argv[]) {
     numberOfThreads = max_threads();
     if (info[0] < 1000000 && numberOfThreads > 32) numberOfThreads = 32;
   }
-  if (algoOption == 0 || algoOption == 1 || algoOption == 5 || algoOption == 7) {
-    fprintf(stderr, "-algo %d is not on the GPU layout path (available: 2, 3, 4, 6, 8)\n", algoOption);
+  if (algoOption == 0 || algoOption == 1) {
+    fprintf(stderr, "-algo %d is not on the GPU layout path (available: 2, 3, 4, 5, 6, 7, 8)\n", algoOption);
     exit(3);
   }
   const int n = (int)info[0];
@@ -187,6 +187,22 @@ int main(int argc, char *argv[]) {
     std::cout << "Barnes-Hut Minbatch Energy:" << out[0] << std::endl;
     std::cout << "Barnes-Hut Minibatch Parallel Wall time required:" << out[1] << std::endl;
     write_out(ctx, "BHMINB" + B + "PARAOUT" + std::to_string(iterations));
+  } else if (algoOption == 5) {
+    algoname = "GREEDY";
+    if (bl_approx_force_directed(ctx, iterations, numberOfThreads, batchsize, out) != BL_OK)
+      die(ctx, "approxForceDirectedAlgorithm");
+    std::cout << "Greedy Approximation" << std::endl;
+    std::cout << "Greedy Approximation Energy:" << out[0] << std::endl;
+    std::cout << "Greedy Approximation Wall time required:" << out[1] << std::endl;
+    write_out(ctx, "GAPPROX" + B + "PARAOUT" + std::to_string(iterations));
+  } else if (algoOption == 7) {
+    algoname = "CACHESD";
+    if (bl_cache_blocking_minibatch_sd(ctx, iterations, numberOfThreads, batchsize, 0, out) != BL_OK)
+      die(ctx, "cacheBlockingminiBatchForceDirectedAlgorithmSD");
+    std::cout << "Cache BlockingSD Minibatch Size:" << batchsize << std::endl;
+    std::cout << "Cache BlockingSD Minbatch Energy:" << out[0] << std::endl;
+    std::cout << "Cache BlockingSD Minibatch Parallel Wall time required:" << out[1] << std::endl;
+    write_out(ctx, "CACHESDMINB" + B + "PARAOUT" + std::to_string(iterations));
   } else if (algoOption == 6) {
     algoname = "BCGRDY";
     if (bl_approx_cache_block_bh(ctx, iterations, numberOfThreads, batchsize, out) != BL_OK)

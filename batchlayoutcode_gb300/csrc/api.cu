@@ -125,13 +125,15 @@ void free_ctx(bl_ctx *c) {
   fr(c->g.rowptr); fr(c->g.colids);
   if (c->g.eff_rowptr != c->g.rowptr) fr(c->g.eff_rowptr);
   if (c->g.eff_colids != c->g.colids) fr(c->g.eff_colids);
+  if (c->g.srt_rowptr != c->g.rowptr) fr(c->g.srt_rowptr);
+  if (c->g.srt_colids != c->g.colids) fr(c->g.srt_colids);
   fr(c->pos); fr(c->force); fr(c->e); fr(c->stage);
   bl::Scratch &s = c->s;
   fr(s.energy_parts); fr(s.energy); fr(s.status); fr(s.partials); fr(s.keys); fr(s.keys_alt);
   fr(s.perm); fr(s.perm_alt); fr(s.hist); fr(s.bbox); fr(s.frame); fr(s.spos); fr(s.bparent);
   fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.qkids); fr(s.lvl_list); fr(s.lvl); fr(s.qcen); fr(s.qbelow); fr(s.startcnt);
   fr(s.startbase); fr(s.scan_tmp); fr(s.nodes); fr(s.nodes_c64); fr(s.nodes_lvl); fr(s.rep);
-  fr(s.stats); fr(s.pos_alt); fr(s.f0); fr(s.cursor);
+  fr(s.stats); fr(s.pos_alt); fr(s.f0); fr(s.cursor); fr(s.cursor_full); fr(s.walk_off); fr(s.walk_pairs);
   for (auto &ls : c->schedules) {
     fr(ls.order);
     fr(ls.d_offsets);
@@ -485,6 +487,46 @@ int bl_approx_cache_block_bh(bl_ctx *ctx, int iterations, int threads, int batch
   return BL_OK;
 }
 
+// Algo 5 from STEP `step`: iterations 0..(int)(0.8*iterations) are the walk
+// phase, the rest the all-pairs phase; STEP *= 0.99 per iteration (:1179).
+static int greedy_loop(bl_ctx *ctx, int iterations, int batch, double step, double *energy) {
+  const int approx = (int)(iterations * 0.8);  // :1086
+  const int first = std::min(iterations, approx + 1);
+  const int rest = iterations - first;
+  if (first > 0)
+    if (int rc = bl::greedy_walk_run(ctx, batch, first, step, 0.99, rest == 0 && energy, energy)) return rc;
+  if (rest > 0) {
+    double s = step;  // STEP after `first` decays, multiplied as the kernel does
+    for (int k = 0; k < first; k++) s = s * 0.99;
+    long long loops = 0;
+    if (int rc = bl::minibatch_run(ctx, bl::MODEL_GREEDY_EXACT, batch, rest, s, 0.99, false, 0.0, 0, energy, &loops))
+      return rc;
+  }
+  return 0;
+}
+
+int bl_approx_force_directed(bl_ctx *ctx, int iterations, int threads, int batch, double *out) {
+  (void)threads;
+  if (!ctx || !out) return BL_ERR_ARG;
+  if (batch < 1) return bl_fail(ctx, BL_ERR_ARG, "batch must be >= 1");
+  BL_CUDA(ctx, cudaSetDevice(ctx->device));
+  const double t0 = wall();
+  if (int rc = init_coordinates(ctx)) return rc;
+  double energy = std::numeric_limits<double>::max();
+  if (int rc = greedy_loop(ctx, iterations, batch, 1.0, &energy)) return rc;
+  collect_timing(ctx);
+  out[0] = energy;
+  out[1] = wall() - t0;
+  return BL_OK;
+}
+
+int bl_cache_blocking_minibatch_sd(bl_ctx *ctx, int iterations, int threads, int batch, int flag,
+                                   double *out) {
+  (void)threads;
+  return minibatch_method(ctx, bl::MODEL_SD, 0.999, iterations, batch, flag, false, out,
+                          std::numeric_limits<double>::max());
+}
+
 int bl_write_to_file(bl_ctx *ctx, const char *tag, char *path_out, int path_cap) {
   if (!ctx || !tag) return BL_ERR_ARG;
   std::vector<double> xy(2 * (size_t)ctx->g.n);
@@ -503,11 +545,21 @@ int bl_write_to_file(bl_ctx *ctx, const char *tag, char *path_out, int path_cap)
 
 int bl_minibatch_iteration(bl_ctx *ctx, int model, int batch, double step, double *energy_out) {
   if (!ctx) return BL_ERR_ARG;
-  if (model != 2 && model != 3 && model != 8) return bl_fail(ctx, BL_ERR_ARG, "model must be 2, 3 or 8");
+  if (model != 2 && model != 3 && model != 8 && model != 7 && model != 5)
+    return bl_fail(ctx, BL_ERR_ARG, "model must be 2, 3, 5, 7 or 8");
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   long long loops = 0;
   double energy = 0.0;
   if (int rc = bl::minibatch_run(ctx, model, batch, 1, step, 1.0, false, 0.0, 0, &energy, &loops)) return rc;
+  if (energy_out) *energy_out = energy;
+  return BL_OK;
+}
+
+int bl_greedy_iteration(bl_ctx *ctx, int batch, double step, double *energy_out) {
+  if (!ctx) return BL_ERR_ARG;
+  BL_CUDA(ctx, cudaSetDevice(ctx->device));
+  double energy = 0.0;
+  if (int rc = bl::greedy_walk_run(ctx, batch, 1, step, 1.0, true, &energy)) return rc;
   if (energy_out) *energy_out = energy;
   return BL_OK;
 }
@@ -579,9 +631,11 @@ int bl_run_resident(bl_ctx *ctx, int algo, int iterations, int batch, double the
   double energy = 0.0;
   long long loops = 0;
   int rc = 0;
-  if (algo == 2 || algo == 3 || algo == 8) {
-    rc = bl::minibatch_run(ctx, algo, batch, iterations, step, algo == 2 ? 0.999 : 0.99, false, 0.0, 0,
-                           &energy, &loops);
+  if (algo == 2 || algo == 3 || algo == 8 || algo == 7) {
+    rc = bl::minibatch_run(ctx, algo, batch, iterations, step, (algo == 2 || algo == 7) ? 0.999 : 0.99, false,
+                           0.0, 0, &energy, &loops);
+  } else if (algo == 5) {
+    rc = greedy_loop(ctx, iterations, batch, step, &energy);
   } else if (algo == 4) {
     if (batch < 1) return bl_fail(ctx, BL_ERR_ARG, "batch must be >= 1");
     double s = step;
@@ -601,7 +655,7 @@ int bl_run_resident(bl_ctx *ctx, int algo, int iterations, int batch, double the
       s = s * 0.999;
     }
   } else {
-    return bl_fail(ctx, BL_ERR_UNSUPPORTED, "bl_run_resident: algo must be 2, 3, 4 or 8");
+    return bl_fail(ctx, BL_ERR_UNSUPPORTED, "bl_run_resident: algo must be 2, 3, 4, 5, 7 or 8");
   }
   if (rc) return rc;
   BL_CUDA(ctx, cudaEventRecord(ctx->run_ev[1], ctx->stream));

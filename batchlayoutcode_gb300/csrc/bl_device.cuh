@@ -15,6 +15,26 @@ __device__ __forceinline__ void rep_pair(float xs, float ys, float xi, float yi,
   fy = fmaf(-dy, r, fy);
 }
 
+// Unit-vector repulsion of source s on target i, the second phase of algo 5
+// (algorithms.cpp:1117-1122): f -= d / |d|, zero for coincident points.
+__device__ __forceinline__ void rep_unit_pair(float xs, float ys, float xi, float yi, float &fx, float &fy) {
+  const float dx = xs - xi, dy = ys - yi;
+  const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
+  const float r = rsqrt_approx(d2);
+  fx = fmaf(-dx, r, fx);
+  fy = fmaf(-dy, r, fy);
+}
+
+// Repulsion law of the minibatch sweep: REP_INV -d/|d|^2 (algo 2/3/7/8),
+// REP_UNIT -d/|d| (algo 5, second phase).
+enum RepLaw { REP_INV = 0, REP_UNIT = 1 };
+
+template <int kRep>
+__device__ __forceinline__ void rep_law_pair(float xs, float ys, float xi, float yi, float &fx, float &fy) {
+  if (kRep == REP_UNIT) rep_unit_pair(xs, ys, xi, yi, fx, fy);
+  else rep_pair(xs, ys, xi, yi, fx, fy);
+}
+
 // Attraction of a matched neighbour, FP32 (algorithms.cpp:759 FR, :912 LinLog, :985 FA).
 __device__ __forceinline__ void attract_pair(int model, float W, float xs, float ys, float xi, float yi,
                                              float &fx, float &fy) {

@@ -132,8 +132,11 @@ struct KernelTimer;  // per-kernel CUDA-event timing (api.cu)
 
 namespace bl {
 
-// Force models of the minibatch sweep (sample/algorithms.cpp:759, :912, :985).
-enum Model { MODEL_FR = 2, MODEL_LINLOG = 3, MODEL_FA = 8 };
+// Force models of the minibatch sweep (sample/algorithms.cpp:759, :912, :985),
+// and the two reference algorithms built on the same sweep: algo 7 (FR over
+// every CSR neighbour, :536-590) and the second phase of algo 5 (FR with
+// unit-vector repulsion, :1112-1125).
+enum Model { MODEL_FR = 2, MODEL_LINLOG = 3, MODEL_FA = 8, MODEL_SD = 7, MODEL_GREEDY_EXACT = 5 };
 
 struct DeviceGraph {
   int n = 0;
@@ -143,6 +146,11 @@ struct DeviceGraph {
   int *eff_rowptr = nullptr;  // neighbours the minibatch cursor actually matches
   int *eff_colids = nullptr;
   int max_eff_degree = 0;
+  // every CSR neighbour, each row sorted ascending with duplicates kept
+  // (aliases the CSR when its rows are sorted); built on first use
+  int *srt_rowptr = nullptr;
+  int *srt_colids = nullptr;
+  int max_degree = -1;  // -1 until srt_* is built
 };
 
 // Level schedule of the Barnes-Hut attraction sweep for one batch size.
@@ -166,6 +174,12 @@ struct Scratch {
   size_t partials_bytes = 0;
   int *cursor = nullptr;  // per (block, vertex) neighbour cursor start
   int cursor_grid = 0;
+  int *cursor_full = nullptr;  // the same for the full sorted rows (algo 7)
+  int cursor_full_grid = 0;
+  // algo 5, first phase: repulsion sources per vertex as (vertex, count) pairs
+  long long *walk_off = nullptr;  // n + 1
+  int2 *walk_pairs = nullptr;
+  long long walk_total = -1;      // -1 until built
   // Barnes-Hut
   size_t bh_n = 0;
   unsigned long long *keys = nullptr, *keys_alt = nullptr;
@@ -257,6 +271,10 @@ int ensure_minibatch_scratch(bl_ctx *ctx, int batch, int grid);
 int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step0,
                   double decay, bool converged, double engt, long long max_loops,
                   double *energy_out, long long *loops_out);
+int ensure_sorted_csr(bl_ctx *ctx);
+int greedy_walks_build(bl_ctx *ctx);
+int greedy_walk_run(bl_ctx *ctx, int batch, int iterations, double step0, double decay, bool want_energy,
+                    double *energy_out);
 int ensure_bh_scratch(bl_ctx *ctx);
 int bh_build(bl_ctx *ctx, const float2 *pos);
 int bh_traverse(bl_ctx *ctx, double theta, bool want_stats, int batch);

@@ -1,7 +1,10 @@
-// minibatch.cu -- all-pairs stochastic minibatch update (algo 2 / 3 / 8).
+// minibatch.cu -- all-pairs stochastic minibatch update (algo 2 / 3 / 8, and
+// algo 7 and the second phase of algo 5).
 //
 // Reference: sample/algorithms.cpp:739-783 (FR), :894-936 (LinLog),
-// :967-1009 (FA).  Vertices are processed in consecutive batches of `batch`
+// :967-1009 (FA), :536-590 (algo 7: attraction over every CSR neighbour, the
+// neighbours' repulsion removed), :1112-1125 (algo 5 after 80 % of the
+// iterations: repulsion -d/|d| instead of -d/|d|^2).  Vertices are processed in consecutive batches of `batch`
 // ids; every force of a batch uses the positions at the start of that batch
 // (Jacobi inside a batch) and the batch then moves by STEP * f/|f| before the
 // next batch starts (Gauss-Seidel across batches).  f_i is attraction over
@@ -159,6 +162,7 @@ __device__ __forceinline__ void cursor_init(Cursor &c, const MinibatchArgs &a, N
 // repulsion the sweep added (identical FP32 operations) and add the model's
 // attraction -- the reference applies attraction instead of repulsion to
 // these pairs (algorithms.cpp:758-768).
+template <int kRep>
 __device__ __noinline__ void correct_neighbours(const MinibatchArgs &a, Cursor c, int ga, int gb,
                                                 const float2 *slice, float2 pi, int sbase, float &fx, float &fy) {
   // bounded by the target's neighbours inside the slice
@@ -167,7 +171,7 @@ __device__ __noinline__ void correct_neighbours(const MinibatchArgs &a, Cursor c
       const float2 pj = slice[q];
       const float dx = pj.x - pi.x, dy = pj.y - pi.y;
       const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
-      const float r = rcp_approx(d2);
+      const float r = (kRep == REP_UNIT) ? rsqrt_approx(d2) : rcp_approx(d2);
       fx = fmaf(dx, r, fx);
       fy = fmaf(dy, r, fy);
       attract_pair(a.model, (float)a.W, pj.x, pj.y, pi.x, pi.y, fx, fy);
@@ -203,6 +207,7 @@ __device__ double block_sum(double v, double *red) {
   return r;
 }
 
+template <int kRep>
 __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int s = blockIdx.x;
@@ -289,27 +294,27 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
         int k = ga;
         if ((k & 1) && k < gb) {
           const float2 q = slice[k];
-          rep_pair(q.x, q.y, p0.x, p0.y, fx0a, fy0a);
-          rep_pair(q.x, q.y, p1.x, p1.y, fx1a, fy1a);
+          rep_law_pair<kRep>(q.x, q.y, p0.x, p0.y, fx0a, fy0a);
+          rep_law_pair<kRep>(q.x, q.y, p1.x, p1.y, fx1a, fy1a);
           k++;
         }
 #pragma unroll 4
         for (; k + 1 < gb; k += 2) {
           const float4 q = *reinterpret_cast<const float4 *>(&slice[k]);
-          rep_pair(q.x, q.y, p0.x, p0.y, fx0a, fy0a);
-          rep_pair(q.z, q.w, p0.x, p0.y, fx0b, fy0b);
-          rep_pair(q.x, q.y, p1.x, p1.y, fx1a, fy1a);
-          rep_pair(q.z, q.w, p1.x, p1.y, fx1b, fy1b);
+          rep_law_pair<kRep>(q.x, q.y, p0.x, p0.y, fx0a, fy0a);
+          rep_law_pair<kRep>(q.z, q.w, p0.x, p0.y, fx0b, fy0b);
+          rep_law_pair<kRep>(q.x, q.y, p1.x, p1.y, fx1a, fy1a);
+          rep_law_pair<kRep>(q.z, q.w, p1.x, p1.y, fx1b, fy1b);
         }
         if (k < gb) {
           const float2 q = slice[k];
-          rep_pair(q.x, q.y, p0.x, p0.y, fx0b, fy0b);
-          rep_pair(q.x, q.y, p1.x, p1.y, fx1b, fy1b);
+          rep_law_pair<kRep>(q.x, q.y, p0.x, p0.y, fx0b, fy0b);
+          rep_law_pair<kRep>(q.x, q.y, p1.x, p1.y, fx1b, fy1b);
         }
         // ... then the matched neighbours in [ga, gb): take their repulsion
         // back (same FP32 formula) and add the model's attraction instead
-        if (v0) correct_neighbours(a, c0r, ga, gb, slice, p0, sbase, fx0b, fy0b);
-        if (v1) correct_neighbours(a, c1r, ga, gb, slice, p1, sbase, fx1b, fy1b);
+        if (v0) correct_neighbours<kRep>(a, c0r, ga, gb, slice, p0, sbase, fx0b, fy0b);
+        if (v1) correct_neighbours<kRep>(a, c1r, ga, gb, slice, p1, sbase, fx1b, fy1b);
         const float2 r0 = make_float2(fx0a + fx0b, fy0a + fy0b);
         const float2 r1 = make_float2(fx1a + fx1b, fy1a + fy1b);
         if (grp > 0) {
@@ -463,6 +468,22 @@ int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step
     if (loops_out) *loops_out = 0;
     return 0;
   }
+  // model 2 / 3 / 8: the cursor-matched neighbours, inverse-distance
+  // repulsion; 7 (algo 7): FR over every CSR neighbour; 5 (algo 5, second
+  // phase): FR over the cursor-matched neighbours, unit-vector repulsion
+  const int attract = (model == MODEL_SD || model == MODEL_GREEDY_EXACT) ? (int)MODEL_FR : model;
+  const bool unit_rep = model == MODEL_GREEDY_EXACT;
+  const bool full_rows = model == MODEL_SD;
+  if (full_rows)
+    if (int rc = ensure_sorted_csr(ctx)) return rc;
+  const int *nb_rowptr = full_rows ? ctx->g.srt_rowptr : ctx->g.eff_rowptr;
+  const int *nb_colids = full_rows ? ctx->g.srt_colids : ctx->g.eff_colids;
+  // the cursor table belongs to one neighbour set; the full rows share the
+  // cursor-matched set's table when the two sets are the same arrays
+  const bool own_table = full_rows && nb_colids != ctx->g.eff_colids;
+  int *&cursor = own_table ? ctx->s.cursor_full : ctx->s.cursor;
+  int &cursor_grid = own_table ? ctx->s.cursor_full_grid : ctx->s.cursor_grid;
+  void (*kernel)(MinibatchArgs) = unit_rep ? minibatch_kernel<REP_UNIT> : minibatch_kernel<REP_INV>;
   int grid = std::min(ctx->num_sms, std::max(1, (n + 127) / 128));
   int dev_smem_optin = 0;
   cudaDeviceGetAttribute(&dev_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
@@ -475,24 +496,23 @@ int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step
   const size_t smem = smem_for(grid);
   if (smem + 1024 > (size_t)dev_smem_optin)
     return bl_fail(ctx, -5, "graph too large for the shared-memory source slices of the minibatch path");
-  BL_CUDA(ctx, cudaFuncSetAttribute(minibatch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  BL_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int occ = 0;
-  BL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, minibatch_kernel, kThreads, smem));
+  BL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kThreads, smem));
   if (occ < 1 || grid > occ * ctx->num_sms)
     return bl_fail(ctx, -5, "minibatch kernel cannot be co-resident");
   if (int rc = ensure_minibatch_scratch(ctx, batch, grid)) return rc;
-  if (ctx->s.cursor_grid != grid) {
-    if (ctx->s.cursor) cudaFree(ctx->s.cursor);
-    ctx->s.cursor = nullptr;
-    ctx->s.cursor_grid = 0;
-    BL_CUDA(ctx, cudaMalloc(&ctx->s.cursor, (size_t)n * grid * sizeof(int)));
+  if (cursor_grid != grid) {
+    if (cursor) cudaFree(cursor);
+    cursor = nullptr;
+    cursor_grid = 0;
+    BL_CUDA(ctx, cudaMalloc(&cursor, (size_t)n * grid * sizeof(int)));
     const long long total = (long long)n * grid;
-    cursor_table_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(ctx->g.eff_rowptr,
-                                                                                ctx->g.eff_colids, n, grid,
-                                                                                ctx->s.cursor);
+    cursor_table_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(nb_rowptr, nb_colids, n, grid,
+                                                                                cursor);
     BL_CUDA(ctx, cudaGetLastError());
     ctx->launches++;
-    ctx->s.cursor_grid = grid;
+    cursor_grid = grid;
   }
   BL_CUDA(ctx, cudaMemsetAsync(ctx->s.status, 0, sizeof(DevStatus), ctx->stream));
   BL_CUDA(ctx, cudaMemsetAsync(ctx->s.partials, 0, (size_t)2 * batch * 2 * sizeof(long long), ctx->stream));
@@ -501,12 +521,12 @@ int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step
   a.n = n;
   a.batch = batch;
   a.nbatches = (n + batch - 1) / batch;
-  a.model = model;
+  a.model = attract;
   a.grid = grid;
   a.W = ctx->weight;
-  a.eff_rowptr = ctx->g.eff_rowptr;
-  a.eff_colids = ctx->g.eff_colids;
-  a.cursor = ctx->s.cursor;
+  a.eff_rowptr = nb_rowptr;
+  a.eff_colids = nb_colids;
+  a.cursor = cursor;
   a.pos = ctx->pos;
   a.force = ctx->force;
   a.e = ctx->e;
@@ -523,8 +543,8 @@ int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step
   a.max_loops = max_loops;
   void *args[] = {&a};
   bl_time_begin(ctx, "minibatch_kernel");
-  BL_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)minibatch_kernel, dim3(grid), dim3(kThreads),
-                                           args, smem, ctx->stream));
+  BL_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)kernel, dim3(grid), dim3(kThreads), args, smem,
+                                           ctx->stream));
   bl_time_end(ctx, "minibatch_kernel");
   ctx->launches++;
   double host[2];
@@ -618,11 +638,11 @@ extern "C" int bl_minibatch_iteration_noalloc(int n, const int *d_rowptr, const 
   if (grid > kNoAllocMaxGrid) return BL_ERR_TOO_LARGE;  // scratch holds 160 blocks of partials
   const size_t smem = smem_for(grid);
   if (smem + 1024 > (size_t)smem_optin) return BL_ERR_TOO_LARGE;
-  if (cudaFuncSetAttribute(minibatch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+  if (cudaFuncSetAttribute(minibatch_kernel<REP_INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return BL_ERR_CUDA;
   int occ = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, minibatch_kernel, kThreads, smem) != cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, minibatch_kernel<REP_INV>, kThreads, smem) != cudaSuccess ||
       occ < 1 || grid > occ * num_sms)
     return BL_ERR_TOO_LARGE;
   // carve the scratch: force accumulators | energy parts | energy + loops | status
@@ -661,7 +681,8 @@ extern "C" int bl_minibatch_iteration_noalloc(int n, const int *d_rowptr, const 
   a.engt = 0.0;
   a.max_loops = 0;
   void *args[] = {&a};
-  if (cudaLaunchCooperativeKernel((const void *)minibatch_kernel, dim3(grid), dim3(kThreads), args, smem, st) !=
+  if (cudaLaunchCooperativeKernel((const void *)minibatch_kernel<REP_INV>, dim3(grid), dim3(kThreads), args, smem,
+                                  st) !=
       cudaSuccess)
     return BL_ERR_CUDA;
   double host_energy = 0.0;

@@ -115,6 +115,16 @@ int bl_barnes_hut_approximation(bl_ctx *ctx, int iterations, int threads, int ba
 /* algo 6: approxCacheBlockBH, :1192-1215 (80% BH at theta 1.2, then algo 2) */
 int bl_approx_cache_block_bh(bl_ctx *ctx, int iterations, int threads, int batch,
                              double *out);
+/* algo 5: approxForceDirectedAlgorithm, :1085-1190 (iterations up to
+ * (int)(0.8*iterations): CSR attraction plus the repulsion of a 200-step
+ * depth-first walk; the rest: all pairs with unit-vector repulsion; STEP
+ * *= 0.99).  Always runs the context's initialiser first, like the reference. */
+int bl_approx_force_directed(bl_ctx *ctx, int iterations, int threads, int batch,
+                             double *out);
+/* algo 7: cacheBlockingminiBatchForceDirectedAlgorithmSD, :517-598
+ * (attraction over every CSR neighbour, repulsion over all other vertices). */
+int bl_cache_blocking_minibatch_sd(bl_ctx *ctx, int iterations, int threads, int batch,
+                                   int flag, double *out);
 
 /* writeToFile (:1244-1256): outputdir + basename(input) + tag + ".txt",
  * lines "x\ty\tid" at 6 significant digits.  The written path is copied to
@@ -124,10 +134,21 @@ int bl_write_to_file(bl_ctx *ctx, const char *tag, char *path_out, int path_cap)
 /* ---- building blocks exposed for verification and benchmarking ----------- */
 
 /* One minibatch iteration (the while-loop body of :742-780 / :895-933 /
- * :968-1006) at the given STEP.  model: 2 FR, 3 LinLog, 8 FA.
+ * :968-1006) at the given STEP.  model: 2 FR, 3 LinLog, 8 FA, 7 (algo 7's
+ * body, :540-590), 5 (algo 5's second-phase body, :1112-1125, :1171-1177).
  * energy_out receives sum |f|^2 of this iteration. */
 int bl_minibatch_iteration(bl_ctx *ctx, int model, int batch, double step,
                            double *energy_out);
+/* One first-phase iteration of algo 5 (:1126-1177) at the given STEP. */
+int bl_greedy_iteration(bl_ctx *ctx, int batch, double step, double *energy_out);
+/* The repulsion sources of algo 5's first phase (the depth-first walks of
+ * :1126-1170; they depend on the graph only) as (source, count) pairs per
+ * vertex: offsets[n+1] (int64), up to `cap` sources and counts; *total =
+ * number of pairs.  A source a walk reaches k times appears with count k
+ * (possibly split over several pairs); pair order within a vertex is not
+ * the walk order. */
+int bl_greedy_walks(bl_ctx *ctx, long long *offsets, int *sources, int *counts,
+                    long long cap, long long *total);
 /* One Barnes-Hut iteration (the loop body of :1039-1071) at the given STEP. */
 int bl_barnes_hut_iteration(bl_ctx *ctx, int batch, double theta, double step,
                             double *energy_out);
@@ -148,8 +169,9 @@ int bl_quadtree(bl_ctx *ctx, int cap, int *lo, int *hi, int *depth, int *nchild,
 int bl_bh_repulsion(bl_ctx *ctx, double theta, double *out, long long *stats);
 
 /* Device-resident run for throughput measurement: `iterations` iterations of
- * algo (2, 3, 4 or 8) from the current device coordinates, no init, no host
- * copies; STEP starts at `step` and decays as in the reference.
+ * algo (2, 3, 4, 5, 7 or 8) from the current device coordinates, no init, no
+ * host copies; STEP starts at `step` and decays as in the reference (algo 5
+ * switches phase after (int)(0.8*iterations) iterations).
  * energy_out = energy of the last iteration; for algo 4 it may be NULL, and
  * then no energy is computed. */
 int bl_run_resident(bl_ctx *ctx, int algo, int iterations, int batch, double theta,

@@ -73,6 +73,9 @@ def lib(fast: bool = False) -> C.CDLL:
     L.orc_forces_on_trajectory.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _f64p, C.c_int, C.c_double,
                                            C.c_double, _f64p, C.c_int]
     L.orc_forces_on_trajectory.restype = C.c_double
+    L.orc_greedy_walks.argtypes = [C.c_int, _i32p, _i32p, np.ctypeslib.ndpointer(np.int64, flags="C"),
+                                   C.c_void_p, C.c_longlong]
+    L.orc_greedy_walks.restype = C.c_longlong
     _libs[fast] = L
     return L
 
@@ -157,7 +160,9 @@ def forces_on_trajectory(algo: int, rowptr, colids, xy_start, xy_end, batch: int
                          weight: float = 1.0, nthreads=None):
     """Forces of one iteration where batch b is evaluated from the state
     {xy_end for earlier batches, xy_start otherwise}: the reference's step
-    re-seeded from another implementation's batch-start states.  -> (forces, energy)"""
+    re-seeded from another implementation's batch-start states.  algo 2, 3,
+    8 (minibatch), 4 (Barnes-Hut), 7 (SD), 5 (greedy, first phase) or 50
+    (greedy, second phase).  -> (forces, energy)"""
     a = np.ascontiguousarray(xy_start, dtype=np.float64)
     b = np.ascontiguousarray(xy_end, dtype=np.float64)
     f = np.zeros_like(a)
@@ -165,3 +170,15 @@ def forces_on_trajectory(algo: int, rowptr, colids, xy_start, xy_end, batch: int
                                        np.ascontiguousarray(colids, np.int32), a.ravel(), b.ravel(), batch, theta,
                                        weight, f.ravel(), _threads(nthreads))
     return f, e
+
+
+def greedy_walks(rowptr, colids):
+    """Algo 5's repulsion sources per vertex -> (offsets int64 [n+1], sources int32)."""
+    rp = np.ascontiguousarray(rowptr, np.int32)
+    ci = np.ascontiguousarray(colids, np.int32)
+    n = rp.shape[0] - 1
+    off = np.zeros(n + 1, np.int64)
+    total = lib().orc_greedy_walks(n, rp, ci, off, None, 0)
+    src = np.zeros(max(total, 1), np.int32)
+    lib().orc_greedy_walks(n, rp, ci, off, src.ctypes.data, total)
+    return off, src[:total]

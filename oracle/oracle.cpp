@@ -370,6 +370,207 @@ double bh_iteration(int n, const int *rowptr, const int *colids, P2 *pos,
   return energy;
 }
 
+// ---------------------------------------------------------------------------
+// Algo 5, greedy approximation (approxForceDirectedAlgorithm,
+// sample/algorithms.cpp:1085-1190).
+//
+// First phase (iterations LOOP <= (int)(0.8 * ITERATIONS), :1110, :1126):
+// f_i = attraction W|d|d over every CSR neighbour of i, plus calcRepulsion
+// (:128-133, -d/|d|^2 when |d|^2 > 0) for every vertex a depth-first walk
+// reaches (:1126-1170): the stack starts with i's neighbours in CSR order;
+// popping u scans u's CSR row and, for each entry v outside {i} u N(i),
+// adds v's repulsion, pushes v and decrements a budget of 200; the walk stops
+// after the row in which the budget reaches 0, or when the stack is empty.
+// Visited vertices are not marked, so a vertex can be reached (and repel)
+// more than once.  The walk depends on the graph only.
+// Second phase (LOOP > approx, :1112-1125): the kindex cursor of algo 2 with
+// attraction W|d|d and repulsion -d/|d| (a unit vector) for every other
+// vertex with |d| > 0, one accumulator over all j.  STEP *= t = 0.99
+// (algorithms.h:44) in both phases.
+// ---------------------------------------------------------------------------
+constexpr int kGreedyBudget = 200;  // countNodes (:1147)
+
+// Repulsion sources of vertex i in walk order (appended to `out`).
+void greedy_walk(int n, const int *rowptr, const int *colids, int i, std::vector<int> &inset,
+                 std::vector<int> &stack, std::vector<int> &out) {
+  (void)n;
+  inset.assign(colids + rowptr[i], colids + rowptr[i + 1]);
+  inset.push_back(i);
+  std::sort(inset.begin(), inset.end());
+  auto member = [&](int v) { return std::binary_search(inset.begin(), inset.end(), v); };
+  stack.assign(colids + rowptr[i], colids + rowptr[i + 1]);
+  int budget = kGreedyBudget;
+  while (!stack.empty()) {
+    const int u = stack.back();
+    stack.pop_back();
+    for (int e = rowptr[u]; e < rowptr[u + 1]; e++) {
+      const int v = colids[e];
+      if (!member(v)) {
+        out.push_back(v);
+        stack.push_back(v);
+        budget--;
+      }
+    }
+    if (budget <= 0) break;
+  }
+}
+
+struct Walks {
+  std::vector<long long> off;  // n + 1
+  std::vector<int> src;
+};
+
+void greedy_walks(int n, const int *rowptr, const int *colids, Walks &w) {
+  w.off.assign(n + 1, 0);
+  w.src.clear();
+  std::vector<int> inset, stack;
+  for (int i = 0; i < n; i++) {
+    greedy_walk(n, rowptr, colids, i, inset, stack, w.src);
+    w.off[i + 1] = (long long)w.src.size();
+  }
+}
+
+// One iteration of the first phase (:1126-1177).
+double greedy_walk_iteration(int n, const int *rowptr, const int *colids, const Walks &w, P2 *pos,
+                             int batch, double W, double step, P2 *force_out, int nthreads,
+                             const P2 *replay = nullptr) {
+  std::vector<P2> prev(n, P2{0.0, 0.0});
+  double energy = 0.0;
+  const int nbatches = (int)std::ceil(1.0 * n / batch);
+  for (int b = 0; b < nbatches; b++) {
+    const int i0 = b * batch, i1 = std::min(n, (b + 1) * batch);
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int i = i0; i < i1; i++) {
+      const P2 pi = pos[i];
+      double fx = 0.0, fy = 0.0;
+      for (int e = rowptr[i]; e < rowptr[i + 1]; e++) {
+        const P2 pj = pos[colids[e]];
+        const double dx = pj.x - pi.x, dy = pj.y - pi.y;
+        const double s = W * std::sqrt(dx * dx + dy * dy);
+        fx += dx * s;
+        fy += dy * s;
+      }
+      for (long long k = w.off[i]; k < w.off[i + 1]; k++) {
+        const P2 pj = pos[w.src[k]];
+        const double dx = pj.x - pi.x, dy = pj.y - pi.y;
+        const double d2 = dx * dx + dy * dy;
+        double tx = 0.0, ty = 0.0;
+        if (d2 > 0) {
+          const double r = 1.0 / d2;
+          tx = tx - dx * r;
+          ty = ty - dy * r;
+        }
+        fx += tx;
+        fy += ty;
+      }
+      prev[i] = P2{fx, fy};
+    }
+    for (int i = i0; i < i1; i++) {
+      if (replay) pos[i] = replay[i];
+      else apply_update(pos[i], prev[i].x, prev[i].y, step);
+      energy += prev[i].x * prev[i].x + prev[i].y * prev[i].y;
+    }
+  }
+  if (force_out)
+    for (int i = 0; i < n; i++) force_out[i] = prev[i];
+  return energy;
+}
+
+// One iteration of the second phase (:1112-1125, :1171-1177).
+double greedy_exact_iteration(int n, const int *rowptr, const int *colids, P2 *pos, int batch, double W,
+                              double step, P2 *force_out, int nthreads, const P2 *replay = nullptr) {
+  const long long nnz = rowptr[n];
+  std::vector<P2> prev(n, P2{0.0, 0.0});
+  double energy = 0.0;
+  const int nbatches = (int)std::ceil(1.0 * n / batch);
+  for (int b = 0; b < nbatches; b++) {
+    const int i0 = b * batch, i1 = std::min(n, (b + 1) * batch);
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int i = i0; i < i1; i++) {
+      const P2 pi = pos[i];
+      long long k = rowptr[i];
+      double fx = 0.0, fy = 0.0;
+      for (int j = 0; j < n; j++) {
+        const double dx = pos[j].x - pi.x, dy = pos[j].y - pi.y;
+        if (k < nnz && j == colids[k]) {
+          const double s = W * std::sqrt(dx * dx + dy * dy);
+          fx += dx * s;
+          fy += dy * s;
+          if (k < (long long)rowptr[i + 1] - 1) k++;
+        } else {
+          const double dist = std::sqrt(dx * dx + dy * dy);
+          if (dist > 0) {
+            const double r = 1.0 / dist;
+            fx = fx - dx * r;
+            fy = fy - dy * r;
+          }
+        }
+      }
+      prev[i] = P2{fx, fy};
+    }
+    for (int i = i0; i < i1; i++) {
+      if (replay) pos[i] = replay[i];
+      else apply_update(pos[i], prev[i].x, prev[i].y, step);
+      energy += prev[i].x * prev[i].x + prev[i].y * prev[i].y;
+    }
+  }
+  if (force_out)
+    for (int i = 0; i < n; i++) force_out[i] = prev[i];
+  return energy;
+}
+
+// ---------------------------------------------------------------------------
+// Algo 7, cacheBlockingminiBatchForceDirectedAlgorithmSD
+// (sample/algorithms.cpp:517-598): every CSR neighbour adds W|d|d + d/|d|^2,
+// then the repulsion d/|d|^2 of every other vertex (j < i, then j > i, no
+// distance guard) is subtracted.  STEP *= 0.999.
+// Deviation: a coincident pair (|d| = 0) contributes 0 here; the reference
+// computes 0 * inf = NaN.
+// ---------------------------------------------------------------------------
+double sd_iteration(int n, const int *rowptr, const int *colids, P2 *pos, int batch, double W, double step,
+                    P2 *force_out, int nthreads, const P2 *replay = nullptr) {
+  std::vector<P2> prev(n, P2{0.0, 0.0});
+  double energy = 0.0;
+  auto inv2 = [](double dx, double dy) {
+    const double d2 = dx * dx + dy * dy;
+    return d2 > 0 ? 1.0 / d2 : 0.0;
+  };
+  const int nbatches = (int)std::ceil(1.0 * n / batch);
+  for (int b = 0; b < nbatches; b++) {
+    const int i0 = b * batch, i1 = std::min(n, (b + 1) * batch);
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int i = i0; i < i1; i++) {
+      const P2 pi = pos[i];
+      double px = 0.0, py = 0.0;
+      for (int e = rowptr[i]; e < rowptr[i + 1]; e++) {
+        const P2 pj = pos[colids[e]];
+        const double dx = pj.x - pi.x, dy = pj.y - pi.y;
+        const double s = W * std::sqrt(dx * dx + dy * dy);
+        const double r = inv2(dx, dy);
+        px += dx * s + dx * r;
+        py += dy * s + dy * r;
+      }
+      double fx = 0.0, fy = 0.0;
+      for (int j = 0; j < n; j++) {
+        if (j == i) continue;
+        const double dx = pos[j].x - pi.x, dy = pos[j].y - pi.y;
+        const double r = inv2(dx, dy);
+        fx += dx * r;
+        fy += dy * r;
+      }
+      prev[i] = P2{px - fx, py - fy};
+    }
+    for (int i = i0; i < i1; i++) {
+      if (replay) pos[i] = replay[i];
+      else apply_update(pos[i], prev[i].x, prev[i].y, step);
+      energy += prev[i].x * prev[i].x + prev[i].y * prev[i].y;
+    }
+  }
+  if (force_out)
+    for (int i = 0; i < n; i++) force_out[i] = prev[i];
+  return energy;
+}
+
 }  // namespace
 
 extern "C" {
@@ -467,7 +668,9 @@ int orc_bh_repulsion(int n, const double *tree_xy, int nq, const double *q_xy,
 //   algo 2 with engt != 0.01 : ...Converged                       (:795-871)
 //   algo 3 : LinLogcacheBlockingminiBatchForceDirectedAlgorithm   (:874-945)
 //   algo 4 : BarnesHutApproximation                              (:1020-1083)
+//   algo 5 : approxForceDirectedAlgorithm                        (:1085-1190)
 //   algo 6 : approxCacheBlockBH                                  (:1192-1215)
+//   algo 7 : cacheBlockingminiBatchForceDirectedAlgorithmSD      (:517-598)
 //   algo 8 : FAcacheBlockingminiBatchForceDirectedAlgorithm       (:947-1018)
 // step_in < 0 means STEP starts at 1.0 (flag == 0); otherwise STEP starts at
 // step_in (the flag == 1 entry of algo 6's second phase, :737).
@@ -529,6 +732,26 @@ int orc_layout(int algo, int n, const int *rowptr, const int *colids,
       step = step * 0.999;
     }
     loops = iterations;
+  } else if (algo == 5) {
+    const int approx = (int)(iterations * 0.8);  // :1086
+    Walks w;
+    greedy_walks(n, rowptr, colids, w);
+    double step = 1.0;
+    for (int it = 0; it < iterations; it++) {
+      if (it > approx)
+        energy = greedy_exact_iteration(n, rowptr, colids, pos, batch, W, step, fo, nthreads);
+      else
+        energy = greedy_walk_iteration(n, rowptr, colids, w, pos, batch, W, step, fo, nthreads);
+      step = step * 0.99;
+      loops++;
+    }
+  } else if (algo == 7) {
+    double step = step_in < 0 ? 1.0 : step_in;
+    for (int it = 0; it < iterations; it++) {
+      energy = sd_iteration(n, rowptr, colids, pos, batch, W, step, fo, nthreads);
+      step = step * 0.999;
+      loops++;
+    }
   } else {
     return -2;
   }
@@ -569,7 +792,27 @@ double orc_forces_on_trajectory(int algo, int n, const int *rowptr, const int *c
   P2 *fo = reinterpret_cast<P2 *>(force_out);
   if (algo == 4)
     return bh_iteration(n, rowptr, colids, pos.data(), batch, theta, W, 1.0, fo, nthreads, rep);
+  if (algo == 7) return sd_iteration(n, rowptr, colids, pos.data(), batch, W, 1.0, fo, nthreads, rep);
+  if (algo == 5) {
+    Walks w;
+    greedy_walks(n, rowptr, colids, w);
+    return greedy_walk_iteration(n, rowptr, colids, w, pos.data(), batch, W, 1.0, fo, nthreads, rep);
+  }
+  if (algo == 50)  // algo 5, second phase
+    return greedy_exact_iteration(n, rowptr, colids, pos.data(), batch, W, 1.0, fo, nthreads, rep);
   return smu_iteration(algo, n, rowptr, colids, pos.data(), batch, W, 1.0, fo, nthreads, rep);
+}
+
+// Repulsion sources of algo 5's first phase for every vertex, in walk order
+// (greedy_walk).  off_out: n + 1 offsets; src_out: up to cap sources (may be
+// NULL).  Returns the total number of sources.
+long long orc_greedy_walks(int n, const int *rowptr, const int *colids, long long *off_out, int *src_out,
+                           long long cap) {
+  Walks w;
+  greedy_walks(n, rowptr, colids, w);
+  std::memcpy(off_out, w.off.data(), (n + 1) * sizeof(long long));
+  if (src_out) std::memcpy(src_out, w.src.data(), std::min<long long>(cap, (long long)w.src.size()) * sizeof(int));
+  return (long long)w.src.size();
 }
 
 }  // extern "C"

@@ -88,6 +88,10 @@ int main(int argc, char **argv) {
       r = al.BarnesHutApproximation(iter, 1, batch, bht, 0);
     else if (algo == 6)
       r = al.approxCacheBlockBH(iter, 1, batch);
+    else if (algo == 5)
+      r = al.approxForceDirectedAlgorithm(iter, 1, batch);
+    else if (algo == 7)
+      r = al.cacheBlockingminiBatchForceDirectedAlgorithmSD(iter, 1, batch, 0);
     std::cout.rdbuf(saved);
     std::string log = sink.str();
     // the converged variant reports its loop count in the output file tag

@@ -11,14 +11,17 @@ Outputs (committed):
   ref_<g>.npz                reference results on them:
     csr_rowptr, csr_colids   the reference reader's CSR
     L<algo>_i<iter>_{xy,f,e} layout outputs after <iter> iterations, batch 32
-                             (coords, per-vertex forces of the last iteration, energy)
+                             (coords, per-vertex forces of the last iteration, energy);
+                             algo 2, 3, 4, 5, 6, 7, 8 at 1 and 4 iterations, algo 5
+                             also at 6 (its second phase)
     conv_{xy,e,loops}        algo 2 with -engt 0.05
     bh_sorted                points after the Morton sort (BarnesHut ctor)
     bh_rep_t<theta>          BH repulsion per vertex at theta 1.2 and 0.5
     tree_*                   the reference quadtree (print_t) in canonical form
     init_greedy              initDFS coordinates
     init_rand1               randInit coordinates with one thread
-  ref_stdout_grid12.txt      stdout of the stock BatchLayout binary (format test)
+  ref_stdout_grid12*.txt     stdout of the stock BatchLayout binary (format test): algo 2
+                             (1 iteration), algo 5 (6 iterations), algo 7 (1 iteration)
 """
 from __future__ import annotations
 
@@ -36,8 +39,9 @@ sys.path.insert(0, ROOT)
 from batchlayoutcode_gb300 import graphs as G  # noqa: E402
 
 BATCH = 32
-ALGOS = (2, 3, 4, 6, 8)
+ALGOS = (2, 3, 4, 5, 6, 7, 8)
 ITERS = (1, 4)
+EXTRA_ITERS = {5: (6,)}  # algo 5 reaches its second phase (LOOP > (int)(0.8 * 6)) at 6 iterations
 
 
 def run(args, cwd=None):
@@ -142,7 +146,7 @@ def main():
         res["csr_colids"] = vals[rows + 1: rows + 1 + nnz].astype(np.int32)
         with tempfile.TemporaryDirectory() as td:
             for algo in ALGOS:
-                for it in ITERS:
+                for it in ITERS + EXTRA_ITERS.get(algo, ()):
                     lines = run([drv, "layout", mtx, initf, str(algo), str(it), str(BATCH), "1.2", "1.0",
                                  "0.01", td + "/"]).splitlines()
                     e = float(lines[0].split()[1])
@@ -173,15 +177,18 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **res)
         print(name, g.n, g.nnz // 2, "ok")
     # stdout layout of the stock CLI (line 18 = wall time, 19 = output path)
-    with tempfile.TemporaryDirectory() as td:
-        mtx = os.path.join(HERE, "grid12.mtx")
-        out = run([stock, "-input", mtx, "-output", td + "/", "-iter", "1", "-algo", "2", "-threads", "1",
-                   "-initf", os.path.join(HERE, "grid12.initf"), "-batch", str(BATCH)], cwd=td)
-        with open(os.path.join(HERE, "ref_stdout_grid12.txt"), "w") as f:
-            f.write(out.replace(td + "/", "<OUTDIR>/").replace(HERE + "/", "<GOLDEN>/"))
-        with open(os.path.join(td, "grid12.mtxCACHEMINB32PARAOUT1.txt")) as fin, \
-                open(os.path.join(HERE, "ref_output_grid12.txt"), "w") as fout:
-            fout.write(fin.read())
+    for algo, iters, name in ((2, 1, "ref_stdout_grid12.txt"), (5, 6, "ref_stdout_grid12_algo5.txt"),
+                              (7, 1, "ref_stdout_grid12_algo7.txt")):
+        with tempfile.TemporaryDirectory() as td:
+            mtx = os.path.join(HERE, "grid12.mtx")
+            out = run([stock, "-input", mtx, "-output", td + "/", "-iter", str(iters), "-algo", str(algo),
+                       "-threads", "1", "-initf", os.path.join(HERE, "grid12.initf"), "-batch", str(BATCH)], cwd=td)
+            with open(os.path.join(HERE, name), "w") as f:
+                f.write(out.replace(td + "/", "<OUTDIR>/").replace(HERE + "/", "<GOLDEN>/"))
+            if algo == 2:
+                with open(os.path.join(td, "grid12.mtxCACHEMINB32PARAOUT1.txt")) as fin, \
+                        open(os.path.join(HERE, "ref_output_grid12.txt"), "w") as fout:
+                    fout.write(fin.read())
 
 
 if __name__ == "__main__":

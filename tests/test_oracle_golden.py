@@ -15,8 +15,7 @@ def gold(request):
     return request.param, load_golden(request.param)
 
 
-@pytest.mark.parametrize("algo", [2, 3, 4, 6, 8])
-@pytest.mark.parametrize("iters", [1, 4])
+@pytest.mark.parametrize("algo,iters", [(a, i) for a in (2, 3, 4, 5, 6, 7, 8) for i in (1, 4)] + [(5, 6)])
 def test_layout_bit_exact(gold, algo, iters):
     _, z = gold
     out, e, loops, f = oracle.layout(algo, z["csr_rowptr"], z["csr_colids"], z["init_xy"], iters, 32,
@@ -64,3 +63,24 @@ def test_bh_repulsion_matches_reference(gold, theta):
     xy = z["init_xy"]
     r = oracle.bh_repulsion(xy, xy, theta, nthreads=2)
     assert np.array_equal(r, z[f"bh_rep_t{theta}"])
+
+
+def test_greedy_walks_follow_the_reference_rules(gold):
+    """Algo 5's walk sources (algorithms.cpp:1126-1170): never i or a
+    neighbour of i, at least 200 pushes unless the stack ran dry, and the
+    overshoot past 200 is bounded by one row."""
+    _, z = gold
+    rp, ci = z["csr_rowptr"], z["csr_colids"]
+    off, src = oracle.greedy_walks(rp, ci)
+    deg = np.diff(rp)
+    n = rp.shape[0] - 1
+    for i in range(n):
+        w = src[off[i]:off[i + 1]]
+        excl = set(ci[rp[i]:rp[i + 1]].tolist()) | {i}
+        assert not (set(w.tolist()) & excl)
+        assert len(w) < 200 + deg.max()
+        if len(w) < 200:  # only when the walk ran out of vertices
+            reach = set()
+            for v in w:
+                reach |= set(ci[rp[v]:rp[v + 1]].tolist())
+            assert reach - excl <= set(w.tolist())
