@@ -180,6 +180,13 @@ struct Scratch {
   long long *walk_off = nullptr;  // n + 1
   int2 *walk_pairs = nullptr;
   long long walk_total = -1;      // -1 until built
+  long long *term_off = nullptr;  // n + 1: CSR entries then walk pairs per vertex
+  int2 *terms = nullptr;          // (source, 0 = attraction | k = k x repulsion)
+  int *term_tgt = nullptr;        // target vertex of each term
+  std::vector<long long> h_term_off;
+  int *greedy_share = nullptr;    // [batches][CTAs + 1] target shares of the cluster's CTAs
+  long long greedy_share_key = -1;
+  float2 *greedy_pos = nullptr;   // second position array (odd number of moves)
   // Barnes-Hut
   size_t bh_n = 0;
   unsigned long long *keys = nullptr, *keys_alt = nullptr;

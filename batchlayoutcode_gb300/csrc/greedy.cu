@@ -17,18 +17,23 @@
 // pushes kept in CSR order by a ballot) merges repeated sources in shared
 // memory and stores each vertex's walk as (source, count) pairs, in a count
 // pass and a fill pass around a prefix sum.  An iteration is then a sparse
-// gather: greedy_iteration_kernel runs all first-phase iterations in one
-// launch of a single thread-block cluster.  For each minibatch, 16 lanes per
-// target sum the attraction over its CSR row and count x repulsion over its
-// pairs (FP32, fixed shuffle tree), a cluster barrier closes the force phase
-// (Jacobi inside the batch), the targets move, and a second cluster barrier
-// publishes the moved positions to the next batch (Gauss-Seidel across
-// batches).  Batches are sequential, so one cluster of 8 or 16 SMs connected
-// by hardware barriers (no spin-waits) does the whole phase; positions
-// (8 B per vertex) stay in L2.
+// gather over a per-vertex term list (CSR entries, then walk pairs):
+// greedy_iteration_kernel runs all first-phase iterations in one launch of a
+// single thread-block cluster (batches are sequential, so one cluster of up
+// to 16 SMs joined by hardware barriers -- no spin-waits -- does the whole
+// phase).  Each CTA takes a share of every batch with about the same number
+// of terms, sums its targets' terms through warp segmented scans into
+// fixed-point shared-memory accumulators (deterministic), and moves its
+// targets; positions alternate between two arrays by the parity of the
+// number of moves, which keeps the batch's start positions readable while
+// it moves (Jacobi inside the batch) and leaves one cluster barrier per
+// batch to publish the moves (Gauss-Seidel across batches).  The next
+// batch's target positions and first terms are loaded during the batch
+// before.  Positions (8 B per vertex) stay in L2.
 //
 // Summation order differs from the reference's (pairs instead of walk
-// order, FP32 instead of FP64): results agree within FP32 rounding.
+// order, FP32 terms summed in warp order and 2^-28 fixed point instead of
+// FP64): results agree within FP32 rounding.
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -168,24 +173,60 @@ __global__ void __launch_bounds__(kWalkThreads) walk_kernel(WalkArgs a) {
 
 // ---- first-phase iterations ----------------------------------------------------
 
+// Term list of a vertex i, at term_off[i] = rowptr[i] + walk_off[i]: its CSR
+// entries as (neighbour, 0) -- attraction -- then its walk pairs as
+// (source, count) -- count x repulsion -- each with its target i.
+__global__ void term_list_kernel(int n, const int *__restrict__ rowptr, const int *__restrict__ colids,
+                                 const long long *__restrict__ walk_off, const int2 *__restrict__ walk_pairs,
+                                 int2 *__restrict__ terms, int *__restrict__ term_tgt) {
+  const int warp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const int i = warp;
+  const int r0 = rowptr[i], r1 = rowptr[i + 1];
+  const long long w0 = walk_off[i], w1 = walk_off[i + 1];
+  const long long q0 = (long long)r0 + w0;
+  for (int k = r0 + lane; k < r1; k += 32) {
+    terms[q0 + (k - r0)] = make_int2(colids[k], 0);
+    term_tgt[q0 + (k - r0)] = i;
+  }
+  const long long qa = q0 + (r1 - r0);
+  for (long long k = w0 + lane; k < w1; k += 32) {
+    terms[qa + (k - w0)] = walk_pairs[k];
+    term_tgt[qa + (k - w0)] = i;
+  }
+}
+
 constexpr int kIterThreads = 512;
-constexpr int kLanes = 16;  // lanes per target
-constexpr int kTargetsPerCta = kIterThreads / kLanes;
+constexpr int kPre = 2;  // terms per thread loaded ahead of each batch
+
+// Fixed-point force accumulators (units of 2^-28, the minibatch sweep's
+// format): integer atomics are exact and order-free, so the per-target sums
+// do not depend on which warp adds first.  A partial beyond +-2^34 is
+// reported instead of wrapping.
+constexpr float kFix = 268435456.0f;
+constexpr double kFixInv = 1.0 / 268435456.0;
+constexpr float kFixLimit = 17179869184.0f;
 
 struct IterArgs {
   int n, batch, nbatches, iterations, energy_last;
   float W;
   double step0, decay;
-  const int *rowptr, *colids;
-  const long long *off;
-  const int2 *pairs;
-  float2 *pos;
+  const long long *term_off;  // per vertex
+  const int2 *terms;
+  const int *term_tgt;
+  const int *share;  // [nbatches][CTAs + 1]: first target (batch-relative) of each CTA's share
+  float2 *pos0, *pos1;  // positions after an even / odd number of moves
   double2 *force;
   double *e;
+  DevStatus *st;
 };
 
-__device__ __forceinline__ void cluster_barrier() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+__device__ __forceinline__ void cluster_arrive() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void cluster_wait() {
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
 __device__ __forceinline__ unsigned int cluster_rank() {
@@ -200,74 +241,176 @@ __device__ __forceinline__ unsigned int cluster_count() {
   return r;
 }
 
-// One launch = one cluster; every thread of every CTA runs the same loop
-// trip counts, so every cluster barrier is reached by all of them.
+__device__ __forceinline__ void fix_add_shared(long long *dst, float v, DevStatus *st) {
+  if (!(fabsf(v) < kFixLimit)) {
+    dev_record_error(st, DEV_FORCE_RANGE);
+    return;
+  }
+  atomicAdd(reinterpret_cast<unsigned long long *>(dst), (unsigned long long)__float2ll_rn(v * kFix));
+}
+
+// One launch = one cluster running every batch of every first-phase
+// iteration.
+//
+// Each CTA owns a share of every batch: a range of consecutive targets whose
+// terms (consecutive in the term list) add up to about 1/CTAs of the batch's
+// terms, so a target's partial sums meet in one CTA's shared memory
+// (warp segmented scans, then fixed-point shared atomics) and the CTA moves
+// its own targets after a CTA barrier.  Jacobi inside the batch without a
+// second cluster barrier: a vertex's position lives in pos0 or pos1 by the
+// parity of the number of times it has moved, so the moves of batch c go to
+// the other array while other CTAs still read the batch's start positions;
+// a reader picks the array from the vertex id (moved once more in this
+// iteration iff it lies before the current batch).  One cluster barrier per
+// batch publishes the moves.  The next batch's share, target positions
+// (staged in shared memory) and first terms are loaded during the batch
+// before (they do not move in it).
 __global__ void __launch_bounds__(kIterThreads, 1) greedy_iteration_kernel(IterArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  long long *acc = reinterpret_cast<long long *>(smem_raw);                // [batch][2]
+  float2 *tpos = reinterpret_cast<float2 *>(acc + 2 * (size_t)a.batch);  // [2][batch]
   const unsigned int rank = cluster_rank(), csize = cluster_count();
-  const int grp = threadIdx.x / kLanes, gl = threadIdx.x % kLanes;
-  const int gt = (int)rank * kTargetsPerCta + grp, ngt = (int)csize * kTargetsPerCta;
-  const int tid = (int)rank * kIterThreads + threadIdx.x, nthr = (int)csize * kIterThreads;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const bool single = a.nbatches == 1;  // the batch moves its own next targets
+  auto P = [&](int moves) { return (moves & 1) ? a.pos1 : a.pos0; };
+  auto share_of = [&](int c, int &lo, int &hi) {
+    lo = __ldg(&a.share[(size_t)c * (csize + 1) + rank]);
+    hi = __ldg(&a.share[(size_t)c * (csize + 1) + rank + 1]);
+  };
+  for (int t = tid; t < 2 * a.batch; t += kIterThreads) acc[t] = 0;
+  // batch 0: share, staged targets, first terms
+  int t_lo, t_hi;
+  share_of(0, t_lo, t_hi);
+  for (int t = t_lo + tid; t < t_hi; t += kIterThreads) tpos[t] = __ldcg(&a.pos0[t]);
+  int2 pt[kPre];
+  int pg[kPre];
+  long long q0, q1;  // this CTA's terms of the batch
+  auto load_terms = [&](int base, int lo, int hi) {
+    q0 = __ldg(&a.term_off[base + lo]);
+    q1 = __ldg(&a.term_off[base + hi]);
+#pragma unroll
+    for (int j = 0; j < kPre; j++) {
+      const long long q = q0 + (long long)j * kIterThreads + tid;
+      pg[j] = -1;
+      if (q < q1) {
+        pt[j] = __ldg(&a.terms[q]);
+        pg[j] = __ldg(&a.term_tgt[q]);
+      }
+    }
+  };
+  load_terms(0, t_lo, t_hi);
+  cluster_arrive();
+  cluster_wait();
   double step = a.step0;
+  unsigned int seq = 0;  // batches processed, for the staging buffer parity
   for (int it = 0; it < a.iterations; it++) {
-    const bool energy_it = a.energy_last && it == a.iterations - 1;
+    const bool last_it = it == a.iterations - 1;
+    const bool energy_it = a.energy_last && last_it;
     const float stepf = (float)step;
-    for (int c = 0; c < a.nbatches; c++) {
+    float2 *const pnew = P(it + 1);
+    for (int c = 0; c < a.nbatches; c++, seq++) {
       const int base = c * a.batch;
-      const int cnt = min(a.batch, a.n - base);
-      // forces of the batch from its start positions
-      for (int t0 = 0; t0 < cnt; t0 += ngt) {  // same trip count in every lane group
-        const int t = t0 + gt;
+      const int buf = (int)(seq & 1u) * a.batch, nbuf = a.batch - buf;
+      // the next batch: its share now, its target positions (unmoved in this
+      // batch unless there is only one batch) staged at the end
+      const int cn = (c + 1 < a.nbatches) ? c + 1 : 0;
+      const int nbase = cn * a.batch;
+      const int nmoves = (cn > c) ? it : it + 1;  // moves of the next targets by then
+      int n_lo, n_hi;
+      share_of(cn, n_lo, n_hi);
+      float2 stage = make_float2(0.f, 0.f);
+      if (!single && n_lo + tid < n_hi) stage = __ldcg(&P(nmoves)[nbase + n_lo + tid]);
+      // ---- partial forces of this CTA's targets from the batch's start ----
+      // a term's contribution, summed per target over the warp's run of
+      // equal targets (segmented inclusive scan), added by the run's last lane
+      auto add_term = [&](int tg, int2 term, float2 pj) {
         float fx = 0.f, fy = 0.f;
-        if (t < cnt) {
-          const int i = base + t;
-          const float2 pi = __ldcg(&a.pos[i]);
-          const int r0 = __ldg(&a.rowptr[i]), r1 = __ldg(&a.rowptr[i + 1]);
-          for (int k = r0 + gl; k < r1; k += kLanes) {
-            const float2 pj = __ldcg(&a.pos[__ldg(&a.colids[k])]);
+        if (tg >= 0) {
+          const float2 pi = tpos[buf + (tg - base)];
+          if (term.y == 0) {
             attract_pair(MODEL_FR, a.W, pj.x, pj.y, pi.x, pi.y, fx, fy);
-          }
-          const long long w0 = __ldg(&a.off[i]), w1 = __ldg(&a.off[i + 1]);
-          for (long long k = w0 + gl; k < w1; k += kLanes) {
-            const int2 p = __ldg(&a.pairs[k]);
-            const float2 pj = __ldcg(&a.pos[p.x]);
+          } else {
             float rx = 0.f, ry = 0.f;
             rep_pair(pj.x, pj.y, pi.x, pi.y, rx, ry);
-            fx = fmaf((float)p.y, rx, fx);
-            fy = fmaf((float)p.y, ry, fy);
+            fx = (float)term.y * rx;
+            fy = (float)term.y * ry;
           }
         }
 #pragma unroll
-        for (int o = kLanes / 2; o > 0; o >>= 1) {
-          fx += __shfl_xor_sync(0xffffffffu, fx, o);
-          fy += __shfl_xor_sync(0xffffffffu, fy, o);
+        for (int o = 1; o < 32; o <<= 1) {
+          const float ux = __shfl_up_sync(0xffffffffu, fx, o);
+          const float uy = __shfl_up_sync(0xffffffffu, fy, o);
+          const int ut = __shfl_up_sync(0xffffffffu, tg, o);
+          if (lane >= o && ut == tg) {
+            fx += ux;
+            fy += uy;
+          }
         }
-        if (t < cnt && gl == 0) a.force[base + t] = make_double2((double)fx, (double)fy);
+        const int nt = __shfl_down_sync(0xffffffffu, tg, 1);
+        if (tg >= 0 && (lane == 31 || nt != tg)) {
+          fix_add_shared(&acc[2 * (tg - base)], fx, a.st);
+          fix_add_shared(&acc[2 * (tg - base) + 1], fy, a.st);
+        }
+      };
+      auto gather = [&](int tg, int j) {
+        return tg >= 0 ? __ldcg(&P(it + (j < base ? 1 : 0))[j]) : make_float2(0.f, 0.f);
+      };
+      // the loaded-ahead terms: every gather issued before the first use
+      float2 pj[kPre];
+#pragma unroll
+      for (int j = 0; j < kPre; j++) pj[j] = gather(pg[j], pt[j].x);
+#pragma unroll
+      for (int j = 0; j < kPre; j++) add_term(pg[j], pt[j], pj[j]);
+      // the rest of the share (CTA-uniform trip count)
+      for (long long q = q0 + (long long)kPre * kIterThreads; q < q1; q += kIterThreads) {
+        int tg = -1;
+        int2 term = make_int2(0, 0);
+        if (q + tid < q1) {
+          term = __ldg(&a.terms[q + tid]);
+          tg = __ldg(&a.term_tgt[q + tid]);
+        }
+        add_term(tg, term, gather(tg, term.x));
       }
-      cluster_barrier();
-      // move the batch (:1171-1177)
-      for (int t = tid; t < cnt; t += nthr) {
+      __syncthreads();
+      // ---- this CTA's targets move (:1171-1177) into the other array ----
+      for (int t = t_lo + tid; t < t_hi; t += kIterThreads) {
         const int i = base + t;
-        const double2 f = __ldcg(&a.force[i]);
-        a.pos[i] = unit_step(__ldcg(&a.pos[i]), f.x, f.y, stepf);
-        if (energy_it) a.e[i] = f.x * f.x + f.y * f.y;
+        const long long vx = acc[2 * t], vy = acc[2 * t + 1];
+        acc[2 * t] = 0;
+        acc[2 * t + 1] = 0;
+        const double dfx = (double)vx * kFixInv, dfy = (double)vy * kFixInv;
+        const float2 np = unit_step(tpos[buf + t], dfx, dfy, stepf);
+        pnew[i] = np;
+        if (single) tpos[nbuf + t] = np;  // this CTA's next targets are the same
+        if (last_it) a.force[i] = make_double2(dfx, dfy);
+        if (energy_it) a.e[i] = dfx * dfx + dfy * dfy;
       }
-      cluster_barrier();
+      if (!single) {
+        if (n_lo + tid < n_hi) tpos[nbuf + n_lo + tid] = stage;
+        for (int t = n_lo + tid + kIterThreads; t < n_hi; t += kIterThreads)
+          tpos[nbuf + t] = __ldcg(&P(nmoves)[nbase + t]);
+      }
+      cluster_arrive();
+      load_terms(nbase, n_lo, n_hi);  // registers only
+      t_lo = n_lo;
+      t_hi = n_hi;
+      cluster_wait();
     }
     step = step * a.decay;
   }
 }
 
-// Largest cluster (16, else 8, 4, 2, 1 CTAs) that can be scheduled.
-int iteration_cluster(bl_ctx *ctx) {
-  static int cached[64] = {0};
-  if (ctx->device >= 0 && ctx->device < 64 && cached[ctx->device]) return cached[ctx->device];
-  cudaFuncSetAttribute(greedy_iteration_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  int best = 1;
-  for (int c : {16, 8, 4, 2}) {
+// Largest cluster (16, else 8, 4, 2, 1 CTAs) of `kernel` with `smem` bytes
+// of dynamic shared memory per CTA that can be scheduled (0: none).
+template <typename Kernel>
+int largest_cluster(Kernel kernel, size_t smem) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (smem) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  for (int c : {16, 8, 4, 2, 1}) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(c);
     cfg.blockDim = dim3(kIterThreads);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = smem;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = c;
@@ -276,14 +419,10 @@ int iteration_cluster(bl_ctx *ctx) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int clusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&clusters, greedy_iteration_kernel, &cfg) == cudaSuccess && clusters >= 1) {
-      best = c;
-      break;
-    }
+    if (cudaOccupancyMaxActiveClusters(&clusters, kernel, &cfg) == cudaSuccess && clusters >= 1) return c;
     cudaGetLastError();  // clear a refused size
   }
-  if (ctx->device >= 0 && ctx->device < 64) cached[ctx->device] = best;
-  return best;
+  return 0;
 }
 
 }  // namespace
@@ -398,35 +537,89 @@ int greedy_walks_build(bl_ctx *ctx) {
   return 0;
 }
 
+int greedy_terms_build(bl_ctx *ctx) {
+  if (ctx->s.terms) return 0;
+  if (int rc = greedy_walks_build(ctx)) return rc;
+  const int n = ctx->g.n;
+  const long long total = ctx->g.nnz + ctx->s.walk_total;
+  // term offsets = CSR offsets + walk offsets
+  std::vector<long long> woff(n + 1);
+  BL_CUDA(ctx, cudaMemcpy(woff.data(), ctx->s.walk_off, (size_t)(n + 1) * sizeof(long long), cudaMemcpyDeviceToHost));
+  for (int i = 0; i <= n; i++) woff[i] += ctx->h_rowptr[i];
+  ctx->s.h_term_off = woff;
+  BL_CUDA(ctx, cudaMalloc(&ctx->s.term_off, (size_t)(n + 1) * sizeof(long long)));
+  BL_CUDA(ctx, cudaMemcpy(ctx->s.term_off, woff.data(), (size_t)(n + 1) * sizeof(long long), cudaMemcpyHostToDevice));
+  BL_CUDA(ctx, cudaMalloc(&ctx->s.term_tgt, (size_t)std::max<long long>(total, 1) * sizeof(int)));
+  BL_CUDA(ctx, cudaMalloc(&ctx->s.terms, (size_t)std::max<long long>(total, 1) * sizeof(int2)));
+  const long long threads = 32LL * n;
+  term_list_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, ctx->stream>>>(
+      n, ctx->g.rowptr, ctx->g.colids, ctx->s.walk_off, ctx->s.walk_pairs, ctx->s.terms, ctx->s.term_tgt);
+  ctx->launches++;
+  BL_CUDA(ctx, cudaGetLastError());
+  return 0;
+}
+
 int greedy_walk_run(bl_ctx *ctx, int batch, int iterations, double step0, double decay, bool want_energy,
                     double *energy_out) {
   const int n = ctx->g.n;
   if (batch < 1) return bl_fail(ctx, BL_ERR_ARG, "batch must be >= 1");
   if (iterations <= 0) return 0;
-  if (int rc = greedy_walks_build(ctx)) return rc;
+  if (int rc = greedy_terms_build(ctx)) return rc;
   if (int rc = bl_check_status(ctx)) return rc;
   batch = std::min(batch, n);
-  const int csize = iteration_cluster(ctx);
+  const size_t smem = (size_t)batch * 2 * sizeof(long long) + (size_t)2 * batch * sizeof(float2);
+  int smem_optin = 0;
+  cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+  if (smem + 1024 > (size_t)smem_optin)
+    return bl_fail(ctx, BL_ERR_TOO_LARGE, "algo 5: batch too large for the shared-memory accumulators");
+  const int csize = largest_cluster(greedy_iteration_kernel, smem);
+  if (csize < 1) return bl_fail(ctx, BL_ERR_TOO_LARGE, "algo 5: no thread-block cluster fits");
+  const int nbatches = (n + batch - 1) / batch;
+  // each CTA's share of every batch: consecutive targets with about
+  // 1/csize of the batch's terms (graph-only; kept for this batch size)
+  if (ctx->s.greedy_share_key != (long long)batch * 64 + csize) {
+    std::vector<int> share((size_t)nbatches * (csize + 1));
+    const std::vector<long long> &to = ctx->s.h_term_off;
+    for (int c = 0; c < nbatches; c++) {
+      const int base = c * batch, cnt = std::min(batch, n - base);
+      const long long q0 = to[base], T = to[base + cnt] - q0;
+      int t = 0;
+      for (int r = 0; r <= csize; r++) {
+        const long long want = (r == csize) ? T : (T * r + csize - 1) / csize;
+        while (t < cnt && to[base + t] - q0 < want) t++;
+        share[(size_t)c * (csize + 1) + r] = (r == csize) ? cnt : t;
+      }
+    }
+    if (ctx->s.greedy_share) cudaFree(ctx->s.greedy_share);
+    ctx->s.greedy_share = nullptr;
+    ctx->s.greedy_share_key = -1;
+    BL_CUDA(ctx, cudaMalloc(&ctx->s.greedy_share, share.size() * sizeof(int)));
+    BL_CUDA(ctx, cudaMemcpy(ctx->s.greedy_share, share.data(), share.size() * sizeof(int), cudaMemcpyHostToDevice));
+    ctx->s.greedy_share_key = (long long)batch * 64 + csize;
+  }
+  if (!ctx->s.greedy_pos) BL_CUDA(ctx, cudaMalloc(&ctx->s.greedy_pos, (size_t)std::max(n, 2) * sizeof(float2)));
   IterArgs a;
   a.n = n;
   a.batch = batch;
-  a.nbatches = (n + batch - 1) / batch;
+  a.nbatches = nbatches;
   a.iterations = iterations;
   a.energy_last = want_energy ? 1 : 0;
   a.W = (float)ctx->weight;
   a.step0 = step0;
   a.decay = decay;
-  a.rowptr = ctx->g.rowptr;
-  a.colids = ctx->g.colids;
-  a.off = ctx->s.walk_off;
-  a.pairs = ctx->s.walk_pairs;
-  a.pos = ctx->pos;
+  a.term_off = ctx->s.term_off;
+  a.terms = ctx->s.terms;
+  a.term_tgt = ctx->s.term_tgt;
+  a.share = ctx->s.greedy_share;
+  a.pos0 = ctx->pos;
+  a.pos1 = ctx->s.greedy_pos;
   a.force = ctx->force;
   a.e = ctx->e;
+  a.st = ctx->s.status;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(csize);
   cfg.blockDim = dim3(kIterThreads);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = ctx->stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -439,6 +632,10 @@ int greedy_walk_run(bl_ctx *ctx, int batch, int iterations, double step0, double
   BL_CUDA(ctx, cudaLaunchKernelEx(&cfg, greedy_iteration_kernel, a));
   bl_time_end(ctx, "greedy_iteration_kernel");
   ctx->launches++;
+  // every vertex moved `iterations` times: an odd count leaves them in pos1
+  if (iterations & 1)
+    BL_CUDA(ctx, cudaMemcpyAsync(ctx->pos, ctx->s.greedy_pos, (size_t)n * sizeof(float2), cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
   if (want_energy) {
     if (int rc = energy_reduce(ctx, energy_out)) return rc;
   } else {

@@ -51,6 +51,13 @@ WORKLOADS = {
                              "largest component; disc init; algo 2 (all-pairs minibatch), batch 256"),
     "grid64": dict(algo=2, batch=256, theta=1.2,
                    desc="64x64 triangulated grid (4,096 vertices, 12,033 edges); disc init; algo 2, batch 256"),
+    "greedy100k": dict(algo=5, batch=256, theta=1.2, graph="chunglu100k", iters_per_step=10,
+                       desc="the 100,000-vertex Chung-Lu graph of chunglu100k; algo 5 (greedy approximation), "
+                            "batch 256; one step = 10 iterations in the reference's phase split (9 with the "
+                            "depth-first-walk repulsion, 1 all-pairs with unit-vector repulsion)"),
+    "sd100k": dict(algo=7, batch=256, theta=1.2, graph="chunglu100k",
+                   desc="the 100,000-vertex Chung-Lu graph of chunglu100k; algo 7 (SD: attraction over every "
+                        "CSR neighbour, all-pairs repulsion), batch 256"),
     "batched256": dict(algo="batched", batch=256, theta=1.2, iterations=30, graphs=256,
                        desc="profiling case of the batched launch: the first 256 graphs of the 2,048-graph mix "
                             "(same generator and seed), 30 iterations"),
@@ -61,7 +68,9 @@ WORKLOADS = {
                              "and algo 4 (bht 1.2) from there, batch 256; one persistent launch replayed as a "
                              "CUDA graph"),
 }
-KERNEL_FOR_ALGO = {4: "traverse_kernel", 2: "minibatch_kernel", 3: "minibatch_kernel", 8: "minibatch_kernel"}
+KERNEL_FOR_ALGO = {4: "traverse_kernel", 2: "minibatch_kernel", 3: "minibatch_kernel", 8: "minibatch_kernel",
+                   7: "minibatch_kernel", 5: "greedy_iteration_kernel"}
+DECAY = {2: 0.999, 4: 0.999, 7: 0.999, 3: 0.99, 8: 0.99, 5: 0.99}
 
 
 def dist_env():
@@ -165,7 +174,7 @@ def l2_bandwidth_gbs(torch, device: int) -> float:
 
 def load_workload(name: str):
     from batchlayoutcode_gb300 import graphs as G
-    return G.cached_workload(name)
+    return G.cached_workload(WORKLOADS.get(name, {}).get("graph", name))
 
 
 def load_batched(seed: int = 1, graphs: int = 2048):
@@ -229,6 +238,8 @@ def baseline_iters(w, n):
     # about 10-30 s of CPU work on a 16-core host
     if w["algo"] == 4:
         return max(2, min(50, int(2.0e7 / max(n, 1))))
+    if w.get("iters_per_step", 1) > 1:  # whole steps, so that the phase split matches
+        return w["iters_per_step"]
     return max(1, min(600, int(2.0e11 / max(n * n, 1))))
 
 
@@ -248,7 +259,8 @@ def run_reference(args, w, g, xy):
                 mtx, initf = os.path.join(td, "w.mtx"), os.path.join(td, "w.initf")
                 G.write_mtx(g, mtx)
                 G.write_initf(xy, initf)
-                it = max(1, min(steps, baseline_iters(w, g.n)))
+                it = baseline_iters(w, g.n) if w.get("iters_per_step", 1) > 1 else \
+                    max(1, min(steps, baseline_iters(w, g.n)))
                 out = subprocess.run([ref_bin, "-input", mtx, "-output", td + "/", "-iter", str(it), "-algo",
                                       str(w["algo"]), "-batch", str(w["batch"]), "-bht", str(w["theta"]),
                                       "-initf", initf, "-threads", str(cores)], cwd=td, capture_output=True,
@@ -263,7 +275,8 @@ def run_reference(args, w, g, xy):
         except (OSError, subprocess.SubprocessError):
             value = None
     if value is None:
-        it = max(1, min(steps, baseline_iters(w, g.n))) * iters_per_step
+        it = baseline_iters(w, g.n) if w.get("iters_per_step", 1) > 1 else \
+            max(1, min(steps, baseline_iters(w, g.n))) * iters_per_step
         value, secs = cpu_baseline_port(g, xy, w, it, cores)
         sample = f"{it} iterations of algo {w['algo']} with the FP64 port (oracle/oracle.cpp, reference " \
                  f"Makefile optimisation flags), same start, {cores} OpenMP threads"
@@ -533,14 +546,15 @@ def main():
     a.nCoordinates = xy
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
     algo, batch, theta = w["algo"], w["batch"], w["theta"]
-    decay = 0.999 if algo in (2, 4) else 0.99
+    ips = w.get("iters_per_step", 1)
+    decay = DECAY[algo] ** ips
     step = 1.0
     # Barnes-Hut steps replay the captured iteration (a CUDA graph, captured
     # during the warm-up); the energy is not read back inside the timed steps
     graph = algo == 4
     a.set_graph_mode(graph)
     for _ in range(args.warmup):
-        a.run_resident(algo, 1, batch, theta, step, want_energy=not graph)
+        a.run_resident(algo, ips, batch, theta, step, want_energy=not graph)
         step *= decay
 
     kernel = KERNEL_FOR_ALGO[algo]
@@ -558,7 +572,7 @@ def main():
         for _ in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
-            a.run_resident(algo, 1, batch, theta, step, want_energy=not graph)
+            a.run_resident(algo, ips, batch, theta, step, want_energy=not graph)
             times.append(a.last_run_ms())
             step *= decay
     torch.cuda.synchronize()
@@ -581,7 +595,7 @@ def main():
         t = torch.tensor([total_ms], device=f"cuda:{device}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
-    value = ws * g.n * args.steps / (total_ms / 1e3)
+    value = ws * g.n * ips * args.steps / (total_ms / 1e3)
     clocks = clk.summary()
 
     # algorithmic bytes of the dominant kernel per launch
@@ -603,6 +617,26 @@ def main():
                 "l2": {"peak": l2, "frac": achieved / l2,
                        "note": "the tree records are read from L1/L2; peak = L2-resident copy bandwidth "
                                "measured in this run"}}
+    elif algo == 5:
+        # per first-phase iteration and vertex: rowptr (8 B), walk offsets
+        # (16 B), own position (8 B), force write + read (32 B), position
+        # write (8 B); per CSR entry: colid + neighbour position (12 B); per
+        # walk pair: (source, count) + source position (16 B)
+        off, _, _ = a.greedy_walks()
+        npairs = float(off[-1])
+        first = min(ips, int(ips * 0.8) + 1)  # walk-phase iterations per launch
+        alg_bytes = first * (72.0 * g.n + 12.0 * g.nnz + 16.0 * npairs)
+        avg_s = kern_ms / max(kern_count, 1) / 1e3
+        achieved = alg_bytes / avg_s / 1e9
+        peak = pk["hbm_gbs"] if pk else 6800.0
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic_from_profile(kernel, args.workload), "kernel": kernel,
+                "kernel_ms_per_launch": avg_s * 1e3, "launches": kern_count,
+                "algorithmic_bytes_per_launch": alg_bytes, "walk_pairs": npairs,
+                "iterations_per_launch": first,
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "fallback",
+                "note": "one cluster runs the batches in sequence, one cluster barrier per batch; "
+                        "positions stay in L2, so the kernel is bound by barrier and gather latency"}
     else:
         pairs = float(g.n) * g.n
         avg_s = kern_ms / max(kern_count, 1) / 1e3
@@ -629,12 +663,14 @@ def main():
         a.set_coordinates_ptr(host_in.data_ptr())
         if algo == 4:
             a.barnes_hut_iteration(batch, theta, step)
+        elif algo == 5:
+            a.run_resident(algo, ips, batch, theta, step)
         else:
             a.minibatch_iteration(algo, batch, step)
         a.get_coordinates_ptr(host_out.data_ptr())
         host_in.copy_(host_out)
     e2e_s = time.perf_counter() - t0
-    e2e = {"value": ws * g.n * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 16 * g.n,
+    e2e = {"value": ws * g.n * ips * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 16 * g.n,
            "d2h_bytes_per_step": 16 * g.n + 8, "steps": e2e_steps}
 
     if rank == 0:
@@ -643,7 +679,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"{args.workload}: {w['desc']}", "vertices": g.n, "edges": g.nnz // 2,
-                       "step": "one layout iteration over the whole graph" +
+                       "step": (f"{ips} layout iterations" if ips > 1 else "one layout iteration") +
+                               " over the whole graph" +
                                (" (replay of the captured iteration, a CUDA graph of its 45 launches)" if graph else ""),
                        "l2": "flushed before every timed step (256 MB write)",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},

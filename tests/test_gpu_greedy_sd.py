@@ -209,3 +209,19 @@ def test_cli_stdout_layout(B, tmp_path, algo, iters, golden):
     assert os.path.exists(str(tmp_path) + f"/grid12.mtx{tag}.txt")
     row = open(tmp_path / "Results.txt").read().strip().split("\t")
     assert row[:2] == [{5: "GREEDY", 7: "CACHESD"}[algo], "FILE"]
+
+
+def test_algo5_first_phase_500k(B):
+    """A 500k-vertex graph (1,926 batches through one cluster): same check
+    as above."""
+    from batchlayoutcode_gb300 import graphs as G
+    g = G.random_geometric(500_000, 6.0, seed=12)
+    xy = G.init_square(g.n, 3).astype(np.float64)
+    with B.Algorithms(g.rowptr, g.colids) as a:
+        a.nCoordinates = xy
+        e = a.greedy_iteration(256, 1.0)
+        f = a.prevCoordinates
+        out = a.nCoordinates
+    tf, te = oracle.forces_on_trajectory(5, g.rowptr, g.colids, xy, out, 256)
+    assert rel_l2(f, tf) <= FORCE_TOL
+    assert abs(e - te) / te <= 2 * FORCE_TOL
