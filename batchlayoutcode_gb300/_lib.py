@@ -28,7 +28,7 @@ EXPORTS = (
     "bl_batched_graph_cycles", "bl_mpnn_set_params", "bl_mpnn_get_params", "bl_mpnn_run",
     "bl_learned_features", "bl_learned_train", "bl_learned_init", "bl_learned_layout",
     "bl_learned_load_model", "bl_approx_force_directed", "bl_cache_blocking_minibatch_sd",
-    "bl_greedy_iteration", "bl_greedy_walks",
+    "bl_greedy_iteration", "bl_greedy_walks", "bl_read_matrix_market_cached",
 )
 
 _lib = None
@@ -110,6 +110,8 @@ def load() -> C.CDLL:
         "bl_cache_blocking_minibatch_sd": (i32, [vp, i32, i32, i32, i32, dp]),
         "bl_greedy_iteration": (i32, [vp, i32, f64, dp]),
         "bl_greedy_walks": (i32, [vp, C.POINTER(C.c_longlong), ip, ip, i64, C.POINTER(C.c_longlong)]),
+        "bl_read_matrix_market_cached": (i32, [cp, cp, C.POINTER(C.c_longlong), dp, C.POINTER(ip), C.POINTER(ip),
+                                               cp, i32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -127,23 +129,30 @@ def _ip(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_int))
 
 
-def read_matrix_market(path: str):
-    """SetInputMatricesAsCSR: -> (rowptr, colids, info dict)."""
+def read_matrix_market(path: str, cache_dir: str | None = None):
+    """SetInputMatricesAsCSR: -> (rowptr, colids, info dict).  With cache_dir,
+    through the binary CSR cache (info["cached"] tells whether it was used)."""
     L = load()
-    info = (C.c_longlong * 4)()
+    info = (C.c_longlong * 5)()
     secs = C.c_double()
     rp = C.POINTER(C.c_int)()
     ci = C.POINTER(C.c_int)()
     err = C.create_string_buffer(512)
-    rc = L.bl_read_matrix_market(path.encode(), info, C.byref(secs), C.byref(rp), C.byref(ci), err, 512)
+    if cache_dir is None:
+        rc = L.bl_read_matrix_market(path.encode(), info, C.byref(secs), C.byref(rp), C.byref(ci), err, 512)
+    else:
+        rc = L.bl_read_matrix_market_cached(path.encode(), cache_dir.encode(), info, C.byref(secs), C.byref(rp),
+                                            C.byref(ci), err, 512)
     if rc != 0:
         raise BatchLayoutError(rc, err.value.decode())
-    rows, cols, nnz, sym = (int(v) for v in info)
+    rows, cols, nnz, sym = (int(v) for v in info[:4])
+    cached = bool(info[4]) if cache_dir is not None else False
     rowptr = np.ctypeslib.as_array(rp, shape=(rows + 1,)).copy()
     colids = np.ctypeslib.as_array(ci, shape=(max(nnz, 1),))[:nnz].copy()
     L.bl_free(C.cast(rp, C.c_void_p))
     L.bl_free(C.cast(ci, C.c_void_p))
-    return rowptr, colids, dict(rows=rows, cols=cols, nnz=nnz, symmetric=bool(sym), seconds=secs.value)
+    return rowptr, colids, dict(rows=rows, cols=cols, nnz=nnz, symmetric=bool(sym), seconds=secs.value,
+                                cached=cached)
 
 
 def random_coordinates(n: int) -> np.ndarray:

@@ -43,6 +43,7 @@ static void helpmessage() {
   printf("-engt <float>, convergenece criteria. It should be a floating point number between 0 to 1 exclusive.\n");
   printf("It indicates if energy value is improved less than this percenrages then optimization will stop and return layout. If this value is set, then number of iteration will be overwritten.\n");
   printf("-weight <float>, a real number to include edge weight.\n");
+  printf("-csrcache <string>, directory of a binary CSR cache of the input (read when it matches the input file, else written).\n");
   printf("-h, show help message.\n");
   printf("default: -weight 1.0 -bht 1.2 -engt 0.01 -batch 256 -iter 600 -threads MAX -algo 2 -init 0\n\n");
 }
@@ -81,7 +82,7 @@ static void write_out(bl_ctx *ctx, const std::string &tag) {
 int main(int argc, char *argv[]) {
   double energyThreshold = 0.01, bhThreshold = 1.2, weight = 1.0;
   int init = 0, batchsize = 256, iterations = 600, numberOfThreads = max_threads(), algoOption = 2;
-  std::string inputfile, initfile, outputfile, algoname = "CACHE", initname = "GREEDY";
+  std::string inputfile, initfile, outputfile, algoname = "CACHE", initname = "GREEDY", csrcache;
   auto arg = [&](int p) -> const char * { return p + 1 < argc ? argv[p + 1] : ""; };
   for (int p = 0; p < argc; p++) {
     if (strcmp(argv[p], "-input") == 0) inputfile = arg(p);
@@ -108,6 +109,7 @@ int main(int argc, char *argv[]) {
       if (energyThreshold < 0.0 || energyThreshold > 1.0) energyThreshold = 0.01;
     }
     if (strcmp(argv[p], "-weight") == 0) weight = atof(arg(p));
+    if (strcmp(argv[p], "-csrcache") == 0) csrcache = arg(p);
     if (strcmp(argv[p], "-h") == 0) {
       helpmessage();
       exit(1);
@@ -124,11 +126,12 @@ int main(int argc, char *argv[]) {
   // SetInputMatricesAsCSR prints these lines (sample/commonutility.h:31-32, IO.h:72-150)
   std::cout << "Reading input matrices in text (ascii)... " << std::endl;
   std::cout << "Input File Directory:" << inputfile << std::endl;
-  long long info[4];
+  long long info[5];
   double secs = 0.0;
   int *rowptr = nullptr, *colids = nullptr;
   char err[512];
-  if (bl_read_matrix_market(inputfile.c_str(), info, &secs, &rowptr, &colids, err, sizeof(err)) != BL_OK) {
+  if (bl_read_matrix_market_cached(inputfile.c_str(), csrcache.empty() ? nullptr : csrcache.c_str(), info, &secs,
+                                   &rowptr, &colids, err, sizeof(err)) != BL_OK) {
     fprintf(stderr, "%s\n", err);
     exit(1);
   }

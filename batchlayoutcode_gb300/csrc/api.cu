@@ -175,16 +175,8 @@ extern "C" {
 
 const char *bl_create_error(void) { return g_create_error.c_str(); }
 
-int bl_read_matrix_market(const char *path, long long *info, double *seconds, int **rowptr,
-                          int **colids, char *err, int errcap) {
-  if (!path || !info || !rowptr || !colids) return BL_ERR_ARG;
-  blhost::MatrixInfo mi;
-  std::vector<int> rp, ci;
-  std::string msg;
-  if (!blhost::read_matrix_market(path, mi, rp, ci, msg)) {
-    if (err && errcap > 0) std::snprintf(err, (size_t)errcap, "%s", msg.c_str());
-    return BL_ERR_IO;
-  }
+static int export_csr(const blhost::MatrixInfo &mi, const std::vector<int> &rp, const std::vector<int> &ci,
+                      long long *info, double *seconds, int **rowptr, int **colids) {
   info[0] = mi.rows;
   info[1] = mi.cols;
   info[2] = mi.nnz;
@@ -200,6 +192,36 @@ int bl_read_matrix_market(const char *path, long long *info, double *seconds, in
   std::memcpy(*rowptr, rp.data(), sizeof(int) * rp.size());
   if (!ci.empty()) std::memcpy(*colids, ci.data(), sizeof(int) * ci.size());
   return BL_OK;
+}
+
+int bl_read_matrix_market(const char *path, long long *info, double *seconds, int **rowptr,
+                          int **colids, char *err, int errcap) {
+  if (!path || !info || !rowptr || !colids) return BL_ERR_ARG;
+  blhost::MatrixInfo mi;
+  std::vector<int> rp, ci;
+  std::string msg;
+  if (!blhost::read_matrix_market(path, mi, rp, ci, msg)) {
+    if (err && errcap > 0) std::snprintf(err, (size_t)errcap, "%s", msg.c_str());
+    return BL_ERR_IO;
+  }
+  return export_csr(mi, rp, ci, info, seconds, rowptr, colids);
+}
+
+int bl_read_matrix_market_cached(const char *path, const char *cache_dir, long long *info, double *seconds,
+                                 int **rowptr, int **colids, char *err, int errcap) {
+  if (!path || !info || !rowptr || !colids) return BL_ERR_ARG;
+  blhost::MatrixInfo mi;
+  std::vector<int> rp, ci;
+  std::string msg;
+  bool cached = false;
+  const bool ok = cache_dir ? blhost::read_matrix_market_cached(path, cache_dir, mi, rp, ci, msg, &cached)
+                            : blhost::read_matrix_market(path, mi, rp, ci, msg);
+  if (!ok) {
+    if (err && errcap > 0) std::snprintf(err, (size_t)errcap, "%s", msg.c_str());
+    return BL_ERR_IO;
+  }
+  info[4] = cached ? 1 : 0;
+  return export_csr(mi, rp, ci, info, seconds, rowptr, colids);
 }
 
 void bl_free(void *p) { std::free(p); }

@@ -2,6 +2,8 @@
 #include "host.h"
 
 #include <stdlib.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <chrono>
@@ -10,6 +12,7 @@
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <thread>
 
 namespace blhost {
 
@@ -118,6 +121,27 @@ bool file_init(const std::string &path, int n, std::vector<double> &xy, std::str
   return true;
 }
 
+// Worker count for the host-side parallel parts: the machine's threads, at
+// most 32, and one per `grain` units of work.
+static int host_threads(size_t work, size_t grain) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t by_work = std::max<size_t>(1, work / std::max<size_t>(grain, 1));
+  return (int)std::min<size_t>({(size_t)hw, (size_t)32, by_work});
+}
+
+template <typename F>
+static void parallel_for(int threads, F &&body) {
+  if (threads <= 1) {
+    body(0);
+    return;
+  }
+  std::vector<std::thread> pool;
+  pool.reserve(threads - 1);
+  for (int k = 1; k < threads; k++) pool.emplace_back(body, k);
+  body(0);
+  for (auto &t : pool) t.join();
+}
+
 bool write_coordinates(const std::string &input, const std::string &outputdir,
                        const std::string &tag, const std::vector<double> &xy,
                        std::string &path_out) {
@@ -126,28 +150,97 @@ bool write_coordinates(const std::string &input, const std::string &outputdir,
   while (std::getline(data, lasttok, '/')) {
   }
   path_out = outputdir + lasttok + tag + ".txt";
-  std::ofstream output(path_out);
-  if (!output) return false;
+  FILE *f = std::fopen(path_out.c_str(), "wb");
+  if (!f) return false;
+  // "x\ty\tid\n" with the default ostream formatting of doubles (6
+  // significant digits, the %g conversion), formatted in parallel slices and
+  // written in order
   const size_t n = xy.size() / 2;
-  for (size_t i = 0; i < n; i++) output << xy[2 * i] << "\t" << xy[2 * i + 1] << "\t" << i + 1 << "\n";
-  return (bool)output;
+  const int T = host_threads(n, 65536);
+  std::vector<std::string> parts(T);
+  parallel_for(T, [&](int k) {
+    const size_t lo = n * k / T, hi = n * (k + 1) / T;
+    std::string &out = parts[k];
+    out.reserve((hi - lo) * 32);
+    char line[96];
+    for (size_t i = lo; i < hi; i++) {
+      const int len = std::snprintf(line, sizeof(line), "%g\t%g\t%zu\n", xy[2 * i], xy[2 * i + 1], i + 1);
+      out.append(line, (size_t)len);
+    }
+  });
+  bool ok = true;
+  for (auto &part : parts)
+    if (!part.empty() && std::fwrite(part.data(), 1, part.size(), f) != part.size()) ok = false;
+  if (std::fclose(f) != 0) ok = false;
+  return ok;
 }
+
+namespace {
+
+// strtol-like base-10 integer at p (leading blanks skipped); returns false
+// when there are no digits.  Saturates instead of overflowing (a saturated
+// value is out of range for any matrix).
+inline bool parse_long(const char *&p, const char *end, long long &v) {
+  while (p < end && (*p == ' ' || *p == '\t' || *p == '\r' || *p == '\v' || *p == '\f')) p++;
+  const char *q = p;
+  bool neg = false;
+  if (q < end && (*q == '+' || *q == '-')) {
+    neg = *q == '-';
+    q++;
+  }
+  if (q >= end || *q < '0' || *q > '9') return false;
+  long long x = 0;
+  while (q < end && *q >= '0' && *q <= '9') {
+    if (x < (1LL << 40)) x = x * 10 + (*q - '0');
+    q++;
+  }
+  v = neg ? -x : x;
+  p = q;
+  return true;
+}
+
+struct ChunkResult {
+  std::vector<std::pair<int, int>> entries;  // 0-based (row, col), file order
+  long long bad_at = -1;                     // entry index (within the chunk) of the first bad line
+  std::string bad_line;
+};
+
+}  // namespace
 
 bool read_matrix_market(const std::string &path, MatrixInfo &info, std::vector<int> &rowptr,
                         std::vector<int> &colids, std::string &msg) {
   const auto t0 = std::chrono::steady_clock::now();
-  std::ifstream in(path);
-  if (!in) {
+  FILE *f = std::fopen(path.c_str(), "rb");
+  if (!f) {
     msg = "cannot open " + path;
     return false;
   }
-  std::string line;
+  std::vector<char> buf;
+  {
+    struct stat st;
+    if (fstat(fileno(f), &st) == 0 && st.st_size > 0) buf.resize((size_t)st.st_size);
+    size_t have = std::fread(buf.data(), 1, buf.size(), f);
+    buf.resize(have);
+    char block[1 << 16];  // anything beyond the size stat reported
+    size_t got;
+    while ((got = std::fread(block, 1, sizeof(block), f)) > 0) buf.insert(buf.end(), block, block + got);
+  }
+  std::fclose(f);
+  const char *text = buf.data();
+  const size_t size = buf.size();
+  // header: comment lines (any of them containing "symmetric" marks the
+  // matrix symmetric, IO.h:67-75), then the size line
   bool symmetric = false;
   int m = 0, ncol = 0;
   long long nnz = -1;
-  while (std::getline(in, line)) {
+  size_t pos = 0;
+  bool have_size = false;
+  while (pos < size) {
+    const char *nl = static_cast<const char *>(std::memchr(text + pos, '\n', size - pos));
+    const size_t eol = nl ? (size_t)(nl - text) : size;
+    std::string line(text + pos, eol - pos);
+    pos = nl ? eol + 1 : size;
     if (!line.empty() && line[0] == '%') {
-      // the reference tests every comment line for "symmetric" (IO.h:67-75)
       if (line.find("symmetric") != std::string::npos) symmetric = true;
       continue;
     }
@@ -155,54 +248,220 @@ bool read_matrix_market(const std::string &path, MatrixInfo &info, std::vector<i
       msg = "bad size line in " + path;
       return false;
     }
+    have_size = true;
     break;
   }
-  if (nnz < 0 || m < 0 || ncol < 0) {
+  if (!have_size || nnz < 0 || m < 0 || ncol < 0) {
     msg = "missing size line in " + path;
     return false;
   }
-  std::vector<std::pair<int, int>> rc;
-  rc.reserve(symmetric ? 2 * nnz : nnz);
-  long long read = 0;
-  while (read < nnz && std::getline(in, line)) {
-    const char *p = line.c_str();
-    char *end = nullptr;
-    const long r = std::strtol(p, &end, 10);
-    if (end == p) continue;  // blank line
-    p = end;
-    const long c = std::strtol(p, &end, 10);
-    if (end == p || r < 1 || c < 1 || r > m || c > ncol) {
-      msg = "bad entry line in " + path + ": " + line;
+  // entry lines, parsed in parallel slices cut at line ends
+  const size_t body = pos, blen = size - pos;
+  const int T = host_threads(blen, 1 << 20);
+  std::vector<size_t> cut(T + 1, size);
+  cut[0] = body;
+  for (int k = 1; k < T; k++) {
+    size_t c = body + blen * k / T;
+    c = std::max(c, cut[k - 1]);
+    const char *nl = c < size ? static_cast<const char *>(std::memchr(text + c, '\n', size - c)) : nullptr;
+    cut[k] = nl ? (size_t)(nl - text) + 1 : size;
+  }
+  std::vector<ChunkResult> res(T);
+  parallel_for(T, [&](int k) {
+    ChunkResult &r = res[k];
+    r.entries.reserve((cut[k + 1] - cut[k]) / 8 + 1);
+    size_t p0 = cut[k];
+    while (p0 < cut[k + 1]) {
+      const char *nl = static_cast<const char *>(std::memchr(text + p0, '\n', cut[k + 1] - p0));
+      const size_t eol = nl ? (size_t)(nl - text) : cut[k + 1];
+      const size_t ls = p0;
+      const char *p = text + p0, *e = text + eol;
+      p0 = eol + 1;
+      long long rr, cc;
+      if (!parse_long(p, e, rr)) continue;  // blank (or comment) line
+      if (!parse_long(p, e, cc) || rr < 1 || cc < 1 || rr > m || cc > ncol) {
+        r.bad_at = (long long)r.entries.size();
+        r.bad_line.assign(text + ls, eol - ls);
+        return;
+      }
+      r.entries.emplace_back((int)rr - 1, (int)cc - 1);
+    }
+  });
+  // only the first nnz entry lines count (the reference stops reading there)
+  long long before = 0;
+  std::vector<long long> keep(T, 0);
+  for (int k = 0; k < T; k++) {
+    const long long have = (long long)res[k].entries.size();
+    if (res[k].bad_at >= 0 && before + res[k].bad_at < nnz) {
+      msg = "bad entry line in " + path + ": " + res[k].bad_line;
       return false;
     }
-    read++;
-    const int ri = (int)r - 1, ci = (int)c - 1;
-    if (symmetric) {
-      if (ri != ci) {
-        rc.emplace_back(ri, ci);
-        rc.emplace_back(ci, ri);
-      }
-    } else {
-      rc.emplace_back(ri, ci);
-    }
+    keep[k] = std::max(0LL, std::min(have, nnz - before));
+    before += have;
+    if (res[k].bad_at >= 0) break;  // lines after a bad one were not parsed
   }
-  if (read < nnz) {
+  if (before < nnz) {
     msg = "file ends before nnz entries in " + path;
     return false;
   }
-  std::vector<int> cnt(m + 1, 0);
-  for (auto &e : rc) cnt[e.first + 1]++;
-  for (int i = 0; i < m; i++) cnt[i + 1] += cnt[i];
-  rowptr = cnt;
-  colids.assign(rc.size(), 0);
-  std::vector<int> fill(cnt.begin(), cnt.end() - 1);
-  for (auto &e : rc) colids[fill[e.first]++] = e.second;
-  for (int i = 0; i < m; i++) std::sort(colids.begin() + rowptr[i], colids.begin() + rowptr[i + 1]);
+  // CSR: symmetric files mirrored with self loops dropped, general files as
+  // they are; rows sorted ascending.  Built without atomics in three
+  // parallel passes: every slice counts its (mirrored) entries per block of
+  // rows, scatters them into a staging array grouped by block (slice order
+  // inside a block), then every block of rows counts, fills and sorts its
+  // own rows, whose colids form one contiguous range.
+  const int NB = std::max(1, std::min(m, 8 * T));  // row blocks
+  const long long bsize = ((long long)m + NB - 1) / NB;
+  auto for_kept = [&](int k, auto &&emit) {
+    for (long long q = 0; q < keep[k]; q++) {
+      const auto &e = res[k].entries[q];
+      if (symmetric) {
+        if (e.first != e.second) {
+          emit(e.first, e.second);
+          emit(e.second, e.first);
+        }
+      } else {
+        emit(e.first, e.second);
+      }
+    }
+  };
+  std::vector<long long> bcnt((size_t)T * NB, 0);  // [slice][block]
+  parallel_for(T, [&](int k) {
+    long long *c = &bcnt[(size_t)k * NB];
+    for_kept(k, [&](int r, int) { c[r / bsize]++; });
+  });
+  std::vector<long long> boff((size_t)T * NB), bbase(NB + 1, 0);
+  long long total = 0;
+  for (int b = 0; b < NB; b++) {
+    bbase[b] = total;
+    for (int k = 0; k < T; k++) {
+      boff[(size_t)k * NB + b] = total;
+      total += bcnt[(size_t)k * NB + b];
+    }
+  }
+  bbase[NB] = total;
+  if (total > 2147483647LL) {
+    msg = "more than 2^31-1 stored entries in " + path;
+    return false;
+  }
+  std::vector<std::pair<int, int>> staged((size_t)total);
+  parallel_for(T, [&](int k) {
+    long long *o = &boff[(size_t)k * NB];
+    for_kept(k, [&](int r, int c) { staged[(size_t)o[r / bsize]++] = std::make_pair(r, c); });
+  });
+  rowptr.assign((size_t)m + 1, 0);
+  colids.assign((size_t)total, 0);
+  const int TB = std::min(NB, T);
+  parallel_for(TB, [&](int k) {
+    for (int b = k; b < NB; b += TB) {
+      const int r0 = (int)std::min<long long>(m, (long long)b * bsize);
+      const int r1 = (int)std::min<long long>(m, (long long)(b + 1) * bsize);
+      std::vector<int> rc(r1 - r0 + 1, 0);
+      for (long long q = bbase[b]; q < bbase[b + 1]; q++) rc[staged[q].first - r0 + 1]++;
+      for (int i = 0; i < r1 - r0; i++) rc[i + 1] += rc[i];
+      for (int i = r0; i < r1; i++) rowptr[i + 1] = (int)(bbase[b] + rc[i - r0 + 1]);
+      std::vector<int> cur(rc.begin(), rc.end() - 1);
+      for (long long q = bbase[b]; q < bbase[b + 1]; q++)
+        colids[(size_t)(bbase[b] + cur[staged[q].first - r0]++)] = staged[q].second;
+      // rows of this block only (rowptr[r0] belongs to the block before)
+      for (int i = r0; i < r1; i++)
+        std::sort(colids.begin() + (bbase[b] + rc[i - r0]), colids.begin() + (bbase[b] + rc[i - r0 + 1]));
+    }
+  });
   info.rows = m;
   info.cols = ncol;
-  info.nnz = (long long)rc.size();
+  info.nnz = (long long)rowptr[m];
   info.symmetric = symmetric;
   info.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return true;
+}
+
+// ---- binary CSR cache ---------------------------------------------------------
+
+namespace {
+constexpr char kCacheMagic[8] = {'B', 'L', 'C', 'S', 'R', '0', '0', '1'};
+
+struct CacheHeader {
+  char magic[8];
+  long long src_size;
+  long long src_mtime_ns;
+  int rows, cols;
+  long long nnz;
+  int symmetric, pad;
+};
+
+bool source_stamp(const std::string &path, long long &size, long long &mtime_ns) {
+  struct stat st;
+  if (stat(path.c_str(), &st) != 0) return false;
+  size = (long long)st.st_size;
+  mtime_ns = (long long)st.st_mtim.tv_sec * 1000000000LL + (long long)st.st_mtim.tv_nsec;
+  return true;
+}
+}  // namespace
+
+std::string csr_cache_path(const std::string &path, const std::string &cache_dir) {
+  std::string base = path;
+  const size_t slash = base.find_last_of('/');
+  if (slash != std::string::npos) base = base.substr(slash + 1);
+  std::string dir = cache_dir;
+  if (!dir.empty() && dir.back() != '/') dir += '/';
+  return dir + base + ".blcsr";
+}
+
+bool read_matrix_market_cached(const std::string &path, const std::string &cache_dir, MatrixInfo &info,
+                               std::vector<int> &rowptr, std::vector<int> &colids, std::string &msg,
+                               bool *from_cache) {
+  const auto t0 = std::chrono::steady_clock::now();
+  if (from_cache) *from_cache = false;
+  long long size = 0, mtime = 0;
+  const bool stamped = source_stamp(path, size, mtime);
+  const std::string cpath = csr_cache_path(path, cache_dir);
+  if (stamped) {
+    if (FILE *f = std::fopen(cpath.c_str(), "rb")) {
+      CacheHeader h;
+      bool ok = std::fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, kCacheMagic, 8) == 0 &&
+                h.src_size == size && h.src_mtime_ns == mtime && h.rows >= 0 && h.nnz >= 0;
+      if (ok) {
+        rowptr.assign((size_t)h.rows + 1, 0);
+        colids.assign((size_t)h.nnz, 0);
+        ok = std::fread(rowptr.data(), sizeof(int), rowptr.size(), f) == rowptr.size() &&
+             (h.nnz == 0 || std::fread(colids.data(), sizeof(int), colids.size(), f) == colids.size()) &&
+             rowptr[0] == 0 && rowptr[h.rows] == h.nnz;
+      }
+      std::fclose(f);
+      if (ok) {
+        info.rows = h.rows;
+        info.cols = h.cols;
+        info.nnz = h.nnz;
+        info.symmetric = h.symmetric != 0;
+        info.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (from_cache) *from_cache = true;
+        return true;
+      }
+    }
+  }
+  if (!read_matrix_market(path, info, rowptr, colids, msg)) return false;
+  if (stamped) {
+    // written to a temporary name and renamed, so a reader never sees half a file
+    const std::string tmp = cpath + ".tmp" + std::to_string((long long)getpid());
+    if (FILE *f = std::fopen(tmp.c_str(), "wb")) {
+      CacheHeader h;
+      std::memset(&h, 0, sizeof(h));
+      std::memcpy(h.magic, kCacheMagic, 8);
+      h.src_size = size;
+      h.src_mtime_ns = mtime;
+      h.rows = info.rows;
+      h.cols = info.cols;
+      h.nnz = info.nnz;
+      h.symmetric = info.symmetric ? 1 : 0;
+      bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 &&
+                std::fwrite(rowptr.data(), sizeof(int), rowptr.size(), f) == rowptr.size() &&
+                (colids.empty() || std::fwrite(colids.data(), sizeof(int), colids.size(), f) == colids.size());
+      ok = (std::fclose(f) == 0) && ok;
+      if (ok) ok = std::rename(tmp.c_str(), cpath.c_str()) == 0;
+      if (!ok) std::remove(tmp.c_str());
+    }
+  }
   return true;
 }
 

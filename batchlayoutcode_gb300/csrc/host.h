@@ -29,7 +29,8 @@ void init_dfs(int n, const std::vector<int> &rowptr, const std::vector<int> &col
 // fileInitialization, sample/algorithms.cpp:98-119.  False when the file
 // cannot be opened.
 bool file_init(const std::string &path, int n, std::vector<double> &xy, std::string &msg);
-// writeToFile, sample/algorithms.cpp:1244-1256.
+// writeToFile, sample/algorithms.cpp:1244-1256; lines formatted in parallel
+// slices and written in order.
 bool write_coordinates(const std::string &input, const std::string &outputdir,
                        const std::string &tag, const std::vector<double> &xy,
                        std::string &path_out);
@@ -45,7 +46,20 @@ struct MatrixInfo {
 // CSR.h:155-186): symmetric files are mirrored with self loops dropped,
 // general files are taken as they are; colids ascend within each row and
 // duplicates are kept.  Values are ignored (the layout never reads them).
+// The file is read whole and its entry lines parsed in parallel slices (one
+// thread per MB, at most 32); the CSR is filled and its rows sorted in
+// parallel.
 bool read_matrix_market(const std::string &path, MatrixInfo &info, std::vector<int> &rowptr,
                         std::vector<int> &colids, std::string &msg);
+
+// The same CSR through a binary cache: <cache_dir>/<basename>.blcsr holds the
+// CSR and the source file's size and modification time; a cache that matches
+// the source is read instead of the text (no parsing), otherwise the text is
+// parsed and the cache (re)written (write failures are ignored).
+// *from_cache (may be null) tells which happened.
+bool read_matrix_market_cached(const std::string &path, const std::string &cache_dir, MatrixInfo &info,
+                               std::vector<int> &rowptr, std::vector<int> &colids, std::string &msg,
+                               bool *from_cache);
+std::string csr_cache_path(const std::string &path, const std::string &cache_dir);
 
 }  // namespace blhost

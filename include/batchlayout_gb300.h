@@ -65,6 +65,15 @@ int bl_num_vertices(const bl_ctx *ctx);
  * On error returns BL_ERR_IO and copies the reason into err (errcap bytes). */
 int bl_read_matrix_market(const char *path, long long *info, double *seconds, int **rowptr,
                           int **colids, char *err, int errcap);
+/* The same through a binary CSR cache (no reference counterpart): with
+ * cache_dir not NULL, <cache_dir>/<basename(path)>.blcsr is read instead of
+ * the text when it records the text file's current size and modification
+ * time, else the text is parsed and the cache written (a failed write is
+ * ignored).  info[4] = 1 when the cache was used, else 0 (info holds 5
+ * values); seconds = load time. */
+int bl_read_matrix_market_cached(const char *path, const char *cache_dir, long long *info,
+                                 double *seconds, int **rowptr, int **colids, char *err,
+                                 int errcap);
 void bl_free(void *p);
 
 /* ---- coordinates (the reference's nCoordinates) ---------------------------- */

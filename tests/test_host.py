@@ -68,6 +68,80 @@ def test_reader_errors(L, tmp_path):
         L.read_matrix_market(str(p))
 
 
+def _csr_reference(n, rows, cols, symmetric):
+    """The reader's CSR built with numpy (mirror + drop self loops when
+    symmetric, rows sorted, duplicates kept)."""
+    r = np.asarray(rows, np.int64) - 1
+    c = np.asarray(cols, np.int64) - 1
+    if symmetric:
+        keep = r != c
+        r, c = np.concatenate([r[keep], c[keep]]), np.concatenate([c[keep], r[keep]])
+    order = np.lexsort((c, r))
+    rp = np.zeros(n + 1, np.int64)
+    np.add.at(rp, r + 1, 1)
+    return np.cumsum(rp).astype(np.int32), c[order].astype(np.int32)
+
+
+def test_reader_parallel_slices_large_file(L, tmp_path):
+    """A 9 MB file parsed in several slices: blank lines, CRLF endings,
+    comment lines after the size line, entries beyond nnz ignored (even a bad
+    one)."""
+    rng = np.random.default_rng(5)
+    n, m = 50000, 400000
+    rows = rng.integers(1, n + 1, m)
+    cols = rng.integers(1, n + 1, m)
+    lines = [f"{a} {b}" for a, b in zip(rows, cols)]
+    for k in range(0, m, 9973):
+        lines[k] += "\r"
+    body = "\n".join(lines[:200000]) + "\n\n% a comment\n   \n" + "\n".join(lines[200000:])
+    p = tmp_path / "big.mtx"
+    p.write_text(f"%%MatrixMarket matrix coordinate pattern symmetric\n{n} {n} {m}\n" + body +
+                 "\n1 1\nthis line is beyond nnz\n")
+    assert p.stat().st_size > 4 << 20
+    rp, ci, info = L.read_matrix_market(str(p))
+    erp, eci = _csr_reference(n, rows, cols, True)
+    assert info["symmetric"] and info["rows"] == n
+    assert np.array_equal(rp, erp) and np.array_equal(ci, eci)
+    # a bad line among the first nnz entries, late in the file, is an error
+    bad = list(lines)
+    bad[m - 5] = "7 0"
+    p.write_text(f"%%MatrixMarket matrix coordinate pattern general\n{n} {n} {m}\n" + "\n".join(bad) + "\n")
+    with pytest.raises(L.BatchLayoutError) as ei:
+        L.read_matrix_market(str(p))
+    assert "7 0" in str(ei.value)
+
+
+def test_reader_binary_cache(L, tmp_path):
+    src = tmp_path / "g.mtx"
+    src.write_text(open(os.path.join(GOLDEN, "rgg.mtx")).read())
+    cache = tmp_path / "cache"
+    cache.mkdir()
+    rp0, ci0, _ = L.read_matrix_market(str(src))
+    rp1, ci1, i1 = L.read_matrix_market(str(src), str(cache))
+    assert not i1["cached"] and (cache / "g.mtx.blcsr").exists()
+    rp2, ci2, i2 = L.read_matrix_market(str(src), str(cache))
+    assert i2["cached"] and i2["symmetric"] == i1["symmetric"] and i2["nnz"] == i1["nnz"]
+    for a, b in ((rp0, rp1), (rp0, rp2), (ci0, ci1), (ci0, ci2)):
+        assert np.array_equal(a, b)
+    # a changed source invalidates the cache
+    src.write_text("%%MatrixMarket matrix coordinate pattern general\n3 3 2\n1 2\n3 1\n")
+    rp3, ci3, i3 = L.read_matrix_market(str(src), str(cache))
+    assert not i3["cached"] and rp3.tolist() == [0, 1, 1, 2] and ci3.tolist() == [1, 0]
+    # an unwritable cache directory still returns the CSR
+    rp4, _, i4 = L.read_matrix_market(str(src), str(tmp_path / "missing_dir"))
+    assert not i4["cached"] and rp4.tolist() == [0, 1, 1, 2]
+
+
+def test_writer_parallel_slices(L, tmp_path):
+    rng = np.random.default_rng(3)
+    xy = rng.normal(0, 100, (300000, 2)) * rng.choice([1e-6, 1.0, 1e6], (300000, 2))
+    path = L.write_coordinates("in.mtx", str(tmp_path) + "/", "T", xy)
+    lines = open(path).read().splitlines()
+    assert len(lines) == len(xy)
+    for i in list(range(0, len(xy), 9973)) + [len(xy) - 1]:
+        assert lines[i] == f"{xy[i, 0]:g}\t{xy[i, 1]:g}\t{i + 1}"
+
+
 @pytest.mark.parametrize("name", GOLDEN_GRAPHS)
 def test_greedy_init_bit_exact(L, name):
     z = load_golden(name)
