@@ -28,7 +28,7 @@ EXPORTS = (
     "bl_batched_graph_cycles", "bl_mpnn_set_params", "bl_mpnn_get_params", "bl_mpnn_run",
     "bl_learned_features", "bl_learned_train", "bl_learned_init", "bl_learned_layout",
     "bl_learned_load_model", "bl_approx_force_directed", "bl_cache_blocking_minibatch_sd",
-    "bl_greedy_iteration", "bl_greedy_walks", "bl_read_matrix_market_cached",
+    "bl_greedy_iteration", "bl_greedy_walks", "bl_read_matrix_market_cached", "bl_bfs_init",
 )
 
 _lib = None
@@ -110,6 +110,7 @@ def load() -> C.CDLL:
         "bl_cache_blocking_minibatch_sd": (i32, [vp, i32, i32, i32, i32, dp]),
         "bl_greedy_iteration": (i32, [vp, i32, f64, dp]),
         "bl_greedy_walks": (i32, [vp, C.POINTER(C.c_longlong), ip, ip, i64, C.POINTER(C.c_longlong)]),
+        "bl_bfs_init": (i32, [vp]),
         "bl_read_matrix_market_cached": (i32, [cp, cp, C.POINTER(C.c_longlong), dp, C.POINTER(ip), C.POINTER(ip),
                                                cp, i32]),
     }
@@ -245,6 +246,10 @@ class Algorithms:
     # ---- initialisers ----
     def randInit(self):
         self._check(self._L.bl_rand_init(self._ctx))
+
+    def bfsInit(self):
+        """Breadth-first greedy start on the GPU (no reference counterpart)."""
+        self._check(self._L.bl_bfs_init(self._ctx))
 
     def initDFS(self):
         self._check(self._L.bl_init_dfs(self._ctx))

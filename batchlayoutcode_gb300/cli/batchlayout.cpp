@@ -43,6 +43,7 @@ static void helpmessage() {
   printf("-engt <float>, convergenece criteria. It should be a floating point number between 0 to 1 exclusive.\n");
   printf("It indicates if energy value is improved less than this percenrages then optimization will stop and return layout. If this value is set, then number of iteration will be overwritten.\n");
   printf("-weight <float>, a real number to include edge weight.\n");
+  printf("-bfsinit, breadth-first greedy initialization on the GPU (overwritten by -initf and -learned).\n");
   printf("-csrcache <string>, directory of a binary CSR cache of the input (read when it matches the input file, else written).\n");
   printf("-h, show help message.\n");
   printf("default: -weight 1.0 -bht 1.2 -engt 0.01 -batch 256 -iter 600 -threads MAX -algo 2 -init 0\n\n");
@@ -110,6 +111,7 @@ int main(int argc, char *argv[]) {
     }
     if (strcmp(argv[p], "-weight") == 0) weight = atof(arg(p));
     if (strcmp(argv[p], "-csrcache") == 0) csrcache = arg(p);
+    if (strcmp(argv[p], "-bfsinit") == 0 && init != 2 && init != 3) init = 4;
     if (strcmp(argv[p], "-h") == 0) {
       helpmessage();
       exit(1);
@@ -122,6 +124,7 @@ int main(int argc, char *argv[]) {
   if (init == 1) initname = "RANDOM";
   if (init == 2) initname = "FILE";
   if (init == 3) initname = "LEARNED";
+  if (init == 4) initname = "BFS";
   banner();
   // SetInputMatricesAsCSR prints these lines (sample/commonutility.h:31-32, IO.h:72-150)
   std::cout << "Reading input matrices in text (ascii)... " << std::endl;

@@ -155,6 +155,7 @@ void free_ctx(bl_ctx *c) {
 
 int init_coordinates(bl_ctx *ctx) {
   if (ctx->init == 0) return bl_init_dfs(ctx);
+  if (ctx->init == 4) return bl_bfs_init(ctx);  // breadth-first start on the GPU
   if (ctx->init == 2) return bl_file_initialization(ctx);
   if (ctx->init == 3) {
     // learned start from the model file in initfile (no reference counterpart)

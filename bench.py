@@ -306,6 +306,9 @@ def time_to_energy(B, g, w, iterations: int = 600):
         fwd_ms, fwd_n = a.kernel_time()
     with B.Algorithms(g.rowptr, g.colids, init=0) as a:
         r0 = a.learnedLayout(np.zeros_like(params), sm, iterations, target, w["batch"], w["theta"], LR.STEP0)
+    # the plain run from the breadth-first greedy start built on the device
+    with B.Algorithms(g.rowptr, g.colids, init=4) as a:
+        e_bfs, bfs_s = a.BarnesHutApproximation(iterations, 0, w["batch"], w["theta"], 0)
     flops = 2.0 * g.n * (32 * 64 + 2 * 128 * 64)
     return {
         "plain_energy": e_plain, "plain_s": plain_s,
@@ -313,11 +316,13 @@ def time_to_energy(B, g, w, iterations: int = 600):
         "learned_start_s": r["init_seconds"], "fell_back": r["fell_back"],
         "speedup": plain_s / r["seconds"] if r["seconds"] > 0 else None,
         "mds_only_s": r0["seconds"], "mds_only_iterations": r0["iterations"], "mds_only_energy": r0["energy"],
+        "bfs_start_plain_s": bfs_s, "bfs_start_plain_energy": e_bfs,
         "mpnn_forward_ms": fwd_ms, "mpnn_forward_tflops": flops / (fwd_ms * 1e-3) / 1e12 if fwd_ms > 0 else None,
         "target": "plain run's final energy x 1.005",
         "note": "wall seconds through the C ABI, starts included (greedy DFS on the host; features, network "
                 "and scale on the device); refinement STEP from 0.3; model batchlayoutcode_gb300/weights/"
-                "mpnn_bh.blw (48 graphs of 1k-100k vertices); mds_only = the same pipeline with a zero network",
+                "mpnn_bh.blw (48 graphs of 1k-100k vertices); mds_only = the same pipeline with a zero network; "
+                "bfs_start_plain = the plain run from the breadth-first start built on the device (bl_bfs_init)",
     }
 
 

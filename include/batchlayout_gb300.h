@@ -93,6 +93,14 @@ int bl_init_dfs(bl_ctx *ctx);
 /* fileInitialization (:98-119): `x y id` lines read with "%lf %lf %d". */
 int bl_file_initialization(bl_ctx *ctx);
 
+/* Breadth-first greedy start (no reference counterpart): initDFS's placement
+ * rule (children of u at 0.1 (cos a, sin a) + (r, r) around it, a stepping by
+ * 360/deg(u), then scaled to a width of 2*MAXMIN) on a breadth-first tree from
+ * vertex 0 (parent = smallest-id neighbour on the previous level), with r a
+ * hash of the vertex id: the whole start on the GPU, deterministic, not the
+ * reference's layout.  Also selected by init = 4 in bl_algorithms_create. */
+int bl_bfs_init(bl_ctx *ctx);
+
 /* Host-only forms of the same initialisers and of writeToFile: no context or
  * GPU needed (xy holds 2*n doubles). */
 int bl_random_coordinates(int n, double *xy);

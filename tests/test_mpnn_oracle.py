@@ -65,3 +65,4 @@ def test_mimic_forward_close_to_fp64():
     a = M.forward(p, rowptr, colids, feats, mimic=True)["xy"]
     b = M.forward(p, rowptr, colids, feats, mimic=False)["xy"]
     assert np.linalg.norm(a - b) / np.linalg.norm(b) < 3e-2
+
