@@ -13,7 +13,8 @@
 //      pass that merges the x-bit level into the y-bit level of the same
 //      digit, giving exactly the reference quadtree without its single-child
 //      chain nodes; centroids are the unweighted means of the children summed
-//      in quadrant order, in FP64, bit-identical to the reference.
+//      in quadrant order, in FP64, bit-identical to the reference, computed
+//      bottom-up by the last-arriving child of every node (no barriers).
 //   4. pre-order layout with skip links: 16-byte records {x, y, D^2, skip}
 //      walked without a stack.
 //   5. repulsion of every vertex in Morton order (coherent warps).  A vertex
@@ -287,13 +288,13 @@ struct TreeArgs {
   double2 *qcen;
   int *qbelow;
   int *startcnt;
-  unsigned int *lvl;    // [33 counts][33 cursors][34 segment offsets]
-  int *lvl_list;        // quad nodes, deepest digit level first
+  int *qpar;     // quad parent of internal node i (index i) and of leaf k (index n-1+k); -1 for the root
+  int *qnchild;  // children of a quad node
+  int *qarrive;  // children whose centroid is done (zero before the pass)
   DevStatus *st;
 };
 
 constexpr int kNoChild = INT_MIN;
-constexpr int kLevels = 33;  // digit levels 0..31 plus 32 for runs of equal keys
 
 
 // Internal node merged into its parent's quad node: the x-bit split of the
@@ -307,115 +308,111 @@ __device__ __forceinline__ bool is_sub(const TreeArgs &t, int node) {
   return (p & 1) && (pp == p - 1);
 }
 
-__device__ __forceinline__ int quad_level(int p) { return p >= 64 ? 32 : (p >> 1); }
-
 // Structure of the quadtree, one thread per sorted position k.  The binary
 // nodes whose range starts at k form the left-child chain above leaf k; the
 // chains of different k are disjoint, so each thread owns its nodes and no
 // synchronisation is needed.  For every quad node on the chain it records the
-// number of quad nodes below it on the chain (qbelow) and its quad children;
-// startcnt[k] counts the quad nodes starting at k.  Digit-level counts are
-// gathered per block for the level-ordered centroid pass.
+// number of quad nodes below it on the chain (qbelow), its quad children, their
+// count, and itself as their quad parent; startcnt[k] counts the quad nodes
+// starting at k.
 __global__ void __launch_bounds__(256) chain_kernel(TreeArgs t) {
-  __shared__ unsigned int hist[kLevels];
-  if (threadIdx.x < kLevels) hist[threadIdx.x] = 0;
-  __syncthreads();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < t.n) {
-    int cnt = 0;
-    int cur = t.parent[t.n - 1 + k];
-    // bounded by the tree height: every step moves to a parent
-    while (cur >= 0 && t.range[cur].x == k) {
-      if (!is_sub(t, cur)) {
-        t.qbelow[cur] = cnt++;
-        int kids[4] = {kNoChild, kNoChild, kNoChild, kNoChild};
-        const int p = t.dlt[cur];
-        if (p < 64) {
-          int m = 0;
-          const int2 ab = t.child[cur];
-          const int sides[2] = {ab.x, ab.y};
+  if (k >= t.n) return;
+  int cnt = 0;
+  int cur = t.parent[t.n - 1 + k];
+  if (k == 0) t.qpar[0] = -1;  // the root
+  // bounded by the tree height: every step moves to a parent
+  while (cur >= 0 && t.range[cur].x == k) {
+    if (!is_sub(t, cur)) {
+      t.qbelow[cur] = cnt++;
+      int kids[4] = {kNoChild, kNoChild, kNoChild, kNoChild};
+      const int p = t.dlt[cur];
+      int m = 0;
+      if (p < 64) {
+        const int2 ab = t.child[cur];
+        const int sides[2] = {ab.x, ab.y};
 #pragma unroll
-          for (int h = 0; h < 2; h++) {
-            const int c = sides[h];
-            if (c >= 0 && is_sub(t, c)) {
-              const int2 cc = t.child[c];
-              kids[m++] = cc.x;
-              kids[m++] = cc.y;
-            } else {
-              kids[m++] = c;
-            }
+        for (int h = 0; h < 2; h++) {
+          const int c = sides[h];
+          if (c >= 0 && is_sub(t, c)) {
+            const int2 cc = t.child[c];
+            kids[m++] = cc.x;
+            kids[m++] = cc.y;
+          } else {
+            kids[m++] = c;
           }
         }
-        t.qkids[cur] = make_int4(kids[0], kids[1], kids[2], kids[3]);
-        atomicAdd(&hist[quad_level(p)], 1u);
+        for (int c = 0; c < m; c++) t.qpar[kids[c] >= 0 ? kids[c] : t.n - 1 + ~kids[c]] = cur;
+      } else {
+        // run of identical keys: every point of the range is a child
+        const int2 rg = t.range[cur];
+        for (int q = rg.x; q <= rg.y; q++) t.qpar[t.n - 1 + q] = cur;
+        m = rg.y - rg.x + 1;
       }
-      cur = (cur == 0) ? -1 : t.parent[cur];
+      t.qkids[cur] = make_int4(kids[0], kids[1], kids[2], kids[3]);
+      t.qnchild[cur] = m;
     }
-    t.startcnt[k] = cnt;
+    cur = (cur == 0) ? -1 : t.parent[cur];
   }
-  __syncthreads();
-  if (threadIdx.x < kLevels && hist[threadIdx.x]) atomicAdd(&t.lvl[threadIdx.x], hist[threadIdx.x]);
+  t.startcnt[k] = cnt;
 }
 
-// segment offsets, deepest level first: seg s holds digit level 32 - s
-__global__ void level_offsets_kernel(unsigned int *lvl) {
-  if (threadIdx.x != 0) return;
-  unsigned int run = 0;
-  for (int s = 0; s < kLevels; s++) {
-    lvl[2 * kLevels + s] = run;
-    run += lvl[32 - s];
-  }
-  lvl[2 * kLevels + kLevels] = run;
-}
+// Centroids bottom-up without waiting.  Every sorted point climbs from its
+// quad parent; at every node the child that arrives last (arrival counter)
+// computes the node's centroid -- the unweighted mean of the children summed
+// in quadrant order in FP64 (BarnesHut.h:197-217), bit-identical to the
+// reference -- and climbs on; the others stop.  A block owns kCenSpan
+// consecutive sorted points, and a binary node whose range lies inside them
+// has its index there too (a Karras node's index is one of its range ends),
+// so the block counts those nodes' arrivals in shared memory with block-scope
+// acquire-release atomics and keeps their centroids in shared memory as
+// well; only nodes that span blocks use global counters (device-scope
+// acquire-release: a node's centroid is stored before its arrival at the
+// parent, the children's are read after the last arrival).
+constexpr int kCenThreads = 1024;
+constexpr int kCenSpan = 2048;  // sorted points per block
 
-__global__ void __launch_bounds__(256) level_fill_kernel(TreeArgs t) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool quad = (i < t.n - 1) && !is_sub(t, i);
-  const int seg = quad ? 32 - quad_level(t.dlt[i]) : -1;
-  const unsigned int active = __ballot_sync(0xffffffffu, quad);
-  if (!quad) return;
-  const unsigned int peers = __match_any_sync(active, seg);
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(peers) - 1;
-  unsigned int base = 0;
-  if (lane == leader) base = atomicAdd(&t.lvl[kLevels + seg], (unsigned int)__popc(peers));
-  base = __shfl_sync(peers, base, leader);
-  const unsigned int rank = __popc(peers & ((1u << lane) - 1u));
-  t.lvl_list[t.lvl[2 * kLevels + seg] + base + rank] = i;
-}
-
-// Centroids, deepest digit level first, with a bounded grid barrier between
-// levels: the unweighted mean of the children summed in quadrant order in
-// FP64 (BarnesHut.h:197-217), bit-identical to the reference.
-__global__ void __launch_bounds__(1024) centroid_kernel(TreeArgs t) {
+__global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
+  __shared__ int s_arrive[kCenSpan];
+  __shared__ double2 s_cen[kCenSpan];
   if (!block_status_ok(t.st)) return;
-  unsigned int epoch = 0;
-  const int gsz = gridDim.x * blockDim.x;
-  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned int *seg_off = t.lvl + 2 * kLevels;
-  int last = -1;
-  for (int sg = 0; sg < kLevels; sg++)
-    if (seg_off[sg + 1] > seg_off[sg]) last = sg;
-  for (int sg = 0; sg <= last; sg++) {
-    const int lo = (int)seg_off[sg], hi = (int)seg_off[sg + 1];
-    if (hi == lo) continue;
-    for (int q = lo + t0; q < hi; q += gsz) {
-      const int node = t.lvl_list[q];
+  const int lo = blockIdx.x * kCenSpan, hi = min(t.n, lo + kCenSpan);
+  for (int q = threadIdx.x; q < kCenSpan; q += kCenThreads) s_arrive[q] = 0;
+  __syncthreads();
+  for (int k = lo + threadIdx.x; k < hi; k += kCenThreads) {
+    int node = t.qpar[t.n - 1 + k];
+    // bounded by the tree height: every step moves to a parent
+    while (node >= 0) {
+      // the node's structure is final (written by earlier kernels)
       const int p = t.dlt[node];
+      const int need = t.qnchild[node];
+      const int4 kk = t.qkids[node];
+      const int2 rg = t.range[node];
+      const int up = t.qpar[node];
+      const bool local = rg.x >= lo && rg.y < hi;
+      int old;
+      if (local) {
+        asm volatile("atom.acq_rel.cta.shared::cta.add.s32 %0, [%1], 1;"
+                     : "=r"(old) : "r"((unsigned)__cvta_generic_to_shared(&s_arrive[node - lo])) : "memory");
+      } else {
+        asm volatile("atom.add.acq_rel.gpu.s32 %0, [%1], 1;" : "=r"(old) : "l"(&t.qarrive[node]) : "memory");
+      }
+      if (old != need - 1) break;
+      // the same FP64 sums as 0.0 + c0 + c1 + ... with the exact steps
+      // (conversions, the first addition, /2 and /4) done in integer
+      // arithmetic: this kernel is bound by the FP64 pipe
       double cx = 0.0, cy = 0.0;
       int cnt = 0;
       if (p >= 64) {
         // run of identical keys: every point is a child (the reference
         // recurses without end here; see the oracle's note)
-        const int2 rg = t.range[node];
-        for (int k = rg.x; k <= rg.y; k++) {
-          const float2 v = t.spos[k];
-          cx = __dadd_rn(cx, (double)v.x);
-          cy = __dadd_rn(cy, (double)v.y);
+        for (int q = rg.x; q <= rg.y; q++) {
+          const float2 v = t.spos[q];
+          cx = cnt ? __dadd_rn(cx, f2d_int(v.x)) : zero_plus(f2d_int(v.x));
+          cy = cnt ? __dadd_rn(cy, f2d_int(v.y)) : zero_plus(f2d_int(v.y));
           cnt++;
         }
       } else {
-        const int4 kk = t.qkids[node];
         const int kids[4] = {kk.x, kk.y, kk.z, kk.w};
 #pragma unroll
         for (int c = 0; c < 4; c++) {
@@ -424,21 +421,25 @@ __global__ void __launch_bounds__(1024) centroid_kernel(TreeArgs t) {
           double vx, vy;
           if (ch < 0) {
             const float2 v = t.spos[~ch];
-            vx = (double)v.x;
-            vy = (double)v.y;
+            vx = f2d_int(v.x);
+            vy = f2d_int(v.y);
           } else {
-            const double2 v = __ldcg(&t.qcen[ch]);
+            // a child inside this block's span was computed here
+            const int2 cr = t.range[ch];
+            const double2 v = (cr.x >= lo && cr.y < hi) ? s_cen[ch - lo] : __ldcg(&t.qcen[ch]);
             vx = v.x;
             vy = v.y;
           }
-          cx = __dadd_rn(cx, vx);
-          cy = __dadd_rn(cy, vy);
+          cx = c ? __dadd_rn(cx, vx) : zero_plus(vx);
+          cy = c ? __dadd_rn(cy, vy) : zero_plus(vy);
           cnt++;
         }
       }
-      t.qcen[node] = make_double2(div_count(cx, cnt), div_count(cy, cnt));
+      const double2 c2 = make_double2(div_count_int(cx, cnt), div_count_int(cy, cnt));
+      t.qcen[node] = c2;
+      if (local) s_cen[node - lo] = c2;
+      node = up;
     }
-    if (sg < last && !grid_barrier(t.st, epoch)) return;
   }
 }
 
@@ -606,8 +607,8 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   if (s.bh_n >= n && s.keys) return 0;
   auto fr = [](void *p) { if (p) cudaFree(p); };
   fr(s.keys); fr(s.keys_alt); fr(s.perm); fr(s.perm_alt); fr(s.hist); fr(s.spos);
-  fr(s.bparent); fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.qkids); fr(s.lvl_list); fr(s.lvl);
-  fr(s.qcen);
+  fr(s.bparent); fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.qkids); fr(s.qpar); fr(s.qnchild);
+  fr(s.qarrive); fr(s.qcen);
   fr(s.qbelow); fr(s.startcnt); fr(s.startbase); fr(s.nodes); fr(s.nodes_c64);
   fr(s.nodes_lvl); fr(s.rep); fr(s.f0); fr(s.pos_alt);
   const size_t nb = (n + kRsTile - 1) / kRsTile;
@@ -624,8 +625,9 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   BL_CUDA(ctx, cudaMalloc(&s.brange, m * sizeof(int2)));
   BL_CUDA(ctx, cudaMalloc(&s.bdelta, m * sizeof(int)));
   BL_CUDA(ctx, cudaMalloc(&s.qkids, m * sizeof(int4)));
-  BL_CUDA(ctx, cudaMalloc(&s.lvl_list, m * sizeof(int)));
-  BL_CUDA(ctx, cudaMalloc(&s.lvl, 3 * 34 * sizeof(unsigned int)));
+  BL_CUDA(ctx, cudaMalloc(&s.qpar, 2 * m * sizeof(int)));
+  BL_CUDA(ctx, cudaMalloc(&s.qnchild, m * sizeof(int)));
+  BL_CUDA(ctx, cudaMalloc(&s.qarrive, m * sizeof(int)));
   BL_CUDA(ctx, cudaMalloc(&s.qcen, m * sizeof(double2)));
   BL_CUDA(ctx, cudaMalloc(&s.qbelow, m * sizeof(int)));
   BL_CUDA(ctx, cudaMalloc(&s.startcnt, (m + 1) * sizeof(int)));
@@ -671,7 +673,7 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   // 8 passes: sorted data is back in keys/perm
   gather_kernel<<<nblk(n, 256), 256, 0, st>>>(pos, s.perm, n, s.spos);
   radix_tree_kernel<<<nblk(n - 1, 256), 256, 0, st>>>(s.keys, n, s.bchild, s.brange, s.bdelta, s.bparent);
-  BL_CUDA(ctx, cudaMemsetAsync(s.lvl, 0, 3 * 34 * sizeof(unsigned int), st));
+  BL_CUDA(ctx, cudaMemsetAsync(s.qarrive, 0, (size_t)n * sizeof(int), st));
   BL_CUDA(ctx, cudaMemsetAsync(s.startcnt + n, 0, sizeof(int), st));
   TreeArgs t;
   t.n = n;
@@ -684,19 +686,13 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   t.qcen = s.qcen;
   t.qbelow = s.qbelow;
   t.startcnt = s.startcnt;
-  t.lvl = s.lvl;
-  t.lvl_list = s.lvl_list;
+  t.qpar = s.qpar;
+  t.qnchild = s.qnchild;
+  t.qarrive = s.qarrive;
   t.st = s.status;
   chain_kernel<<<nblk(n, 256), 256, 0, st>>>(t);
-  level_offsets_kernel<<<1, 32, 0, st>>>(s.lvl);
-  level_fill_kernel<<<nblk(n - 1, 256), 256, 0, st>>>(t);
-  BL_CUDA(ctx, cudaMemsetAsync(&s.status->barrier, 0, sizeof(unsigned int), st));
-  {
-    void *args[] = {&t};
-    BL_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)centroid_kernel, dim3(ctx->num_sms), dim3(1024), args,
-                                             0, st));
-  }
-  ctx->launches += 6;
+  centroid_kernel<<<nblk(n, kCenSpan), kCenThreads, 0, st>>>(t);
+  ctx->launches += 4;
   if (int rc = scan_exclusive_int(ctx, s.startcnt, s.startbase, n + 1)) return rc;
   LayoutArgs L;
   L.n = n;

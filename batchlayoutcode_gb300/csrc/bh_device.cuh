@@ -84,6 +84,42 @@ __device__ __forceinline__ double div_count(double x, int c) {
   return __ddiv_rn(x, (double)c);
 }
 
+// The same quotient with integer operations where they are exact, so that the
+// FP64 pipe (a small fraction of the FP32 rate on this part) only sees the
+// division by 3 and the run lengths: x/2 and x/4 lower the exponent of a
+// normal x (and leave +-0 alone); anything else takes div_count.
+__device__ __forceinline__ double div_count_int(double x, int c) {
+  if (c == 2 || c == 4) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned int e = (unsigned int)(b >> 52) & 0x7ffu;
+    const unsigned int k = c == 2 ? 1u : 2u;
+    if ((b << 1) == 0ull) return x;  // +-0
+    if (e > k && e < 0x7ffu) return __longlong_as_double((long long)(b - ((unsigned long long)k << 52)));
+  }
+  return div_count(x, c);
+}
+
+// float -> double without the conversion instruction (exact; the bits are
+// rebiased and shifted): normal floats and +-0; subnormal, infinite and NaN
+// floats take the conversion.
+__device__ __forceinline__ double f2d_int(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int e = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  if (e == 0u) {
+    if (u & 0x7fffffu) return (double)f;
+    return __longlong_as_double((long long)sign);
+  }
+  if (e == 0xffu) return (double)f;
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
+// 0.0 + x exactly: x, except that -0 becomes +0.
+__device__ __forceinline__ double zero_plus(double x) {
+  return (__double_as_longlong(x) == (long long)0x8000000000000000ll) ? 0.0 : x;
+}
+
 // Loads of the tree records and positions: through the read-only data cache
 // (kRO) when the launch does not write them, plain loads otherwise (the
 // one-block path rewrites them every iteration, ordered by block barriers).

@@ -201,8 +201,9 @@ struct Scratch {
   int2 *brange = nullptr;        // [first, last] of internal node
   int *bdelta = nullptr;         // common prefix length of internal node
   int4 *qkids = nullptr;         // quad children of a quad node
-  int *lvl_list = nullptr;       // quad nodes ordered by digit level, deepest first
-  unsigned int *lvl = nullptr;   // level counts, cursors, segment offsets
+  int *qpar = nullptr;           // quad parent of a quad node / leaf
+  int *qnchild = nullptr;        // number of children of a quad node
+  int *qarrive = nullptr;        // children finished (bottom-up centroid pass)
   double2 *qcen = nullptr;       // centroid of quad node (indexed by binary internal id)
   int *qbelow = nullptr;         // chain length below a quad node
   int *startcnt = nullptr;       // quad nodes starting at each sorted position (n+1)
