@@ -357,89 +357,140 @@ __global__ void __launch_bounds__(256) chain_kernel(TreeArgs t) {
   t.startcnt[k] = cnt;
 }
 
-// Centroids bottom-up without waiting.  Every sorted point climbs from its
-// quad parent; at every node the child that arrives last (arrival counter)
-// computes the node's centroid -- the unweighted mean of the children summed
-// in quadrant order in FP64 (BarnesHut.h:197-217), bit-identical to the
-// reference -- and climbs on; the others stop.  A block owns kCenSpan
-// consecutive sorted points, and a binary node whose range lies inside them
-// has its index there too (a Karras node's index is one of its range ends),
-// so the block counts those nodes' arrivals in shared memory with block-scope
-// acquire-release atomics and keeps their centroids in shared memory as
-// well; only nodes that span blocks use global counters (device-scope
-// acquire-release: a node's centroid is stored before its arrival at the
-// parent, the children's are read after the last arrival).
+// Centroids bottom-up, without grid barriers or waits.  The centroid of a
+// quad node is the unweighted mean of its children summed in quadrant order
+// in FP64 (BarnesHut.h:197-217), bit-identical to the reference; it can be
+// computed once every child is done.  A block owns kCenSpan consecutive
+// sorted points; a binary node whose range lies inside them has its index
+// there too (a Karras node's index is one of its range ends), so the block
+// keeps those nodes' arrival counters and centroids in shared memory and
+// processes them in rounds: the nodes whose children are all done form a
+// queue, handled one node per thread so that the FP64 work (a small fraction
+// of the FP32 rate on this part, charged per warp instruction) runs in full
+// warps, and a node's last arriving child appends it to the next round's
+// queue.  A node that spans blocks is computed by the thread whose arrival
+// at it (device-scope acquire-release counter) is the last, which climbs on
+// from there: such nodes are few.
 constexpr int kCenThreads = 1024;
 constexpr int kCenSpan = 2048;  // sorted points per block
 
-__global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
-  __shared__ int s_arrive[kCenSpan];
-  __shared__ double2 s_cen[kCenSpan];
-  if (!block_status_ok(t.st)) return;
-  const int lo = blockIdx.x * kCenSpan, hi = min(t.n, lo + kCenSpan);
-  for (int q = threadIdx.x; q < kCenSpan; q += kCenThreads) s_arrive[q] = 0;
-  __syncthreads();
-  for (int k = lo + threadIdx.x; k < hi; k += kCenThreads) {
-    int node = t.qpar[t.n - 1 + k];
-    // bounded by the tree height: every step moves to a parent
-    while (node >= 0) {
-      // the node's structure is final (written by earlier kernels)
-      const int p = t.dlt[node];
-      const int need = t.qnchild[node];
-      const int4 kk = t.qkids[node];
-      const int2 rg = t.range[node];
-      const int up = t.qpar[node];
-      const bool local = rg.x >= lo && rg.y < hi;
-      int old;
-      if (local) {
-        asm volatile("atom.acq_rel.cta.shared::cta.add.s32 %0, [%1], 1;"
-                     : "=r"(old) : "r"((unsigned)__cvta_generic_to_shared(&s_arrive[node - lo])) : "memory");
-      } else {
-        asm volatile("atom.add.acq_rel.gpu.s32 %0, [%1], 1;" : "=r"(old) : "l"(&t.qarrive[node]) : "memory");
-      }
-      if (old != need - 1) break;
-      // the same FP64 sums as 0.0 + c0 + c1 + ... with the exact steps
-      // (conversions, the first addition, /2 and /4) done in integer
-      // arithmetic: this kernel is bound by the FP64 pipe
-      double cx = 0.0, cy = 0.0;
-      int cnt = 0;
-      if (p >= 64) {
-        // run of identical keys: every point is a child (the reference
-        // recurses without end here; see the oracle's note)
-        for (int q = rg.x; q <= rg.y; q++) {
-          const float2 v = t.spos[q];
-          cx = cnt ? __dadd_rn(cx, f2d_int(v.x)) : zero_plus(f2d_int(v.x));
-          cy = cnt ? __dadd_rn(cy, f2d_int(v.y)) : zero_plus(f2d_int(v.y));
-          cnt++;
-        }
-      } else {
-        const int kids[4] = {kk.x, kk.y, kk.z, kk.w};
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-          const int ch = kids[c];
-          if (ch == kNoChild) break;
-          double vx, vy;
-          if (ch < 0) {
-            const float2 v = t.spos[~ch];
-            vx = f2d_int(v.x);
-            vy = f2d_int(v.y);
-          } else {
-            // a child inside this block's span was computed here
-            const int2 cr = t.range[ch];
-            const double2 v = (cr.x >= lo && cr.y < hi) ? s_cen[ch - lo] : __ldcg(&t.qcen[ch]);
-            vx = v.x;
-            vy = v.y;
-          }
-          cx = c ? __dadd_rn(cx, vx) : zero_plus(vx);
-          cy = c ? __dadd_rn(cy, vy) : zero_plus(vy);
-          cnt++;
-        }
-      }
-      const double2 c2 = make_double2(div_count_int(cx, cnt), div_count_int(cy, cnt));
-      t.qcen[node] = c2;
-      if (local) s_cen[node - lo] = c2;
-      node = up;
+struct CenSmem {
+  double2 cen[kCenSpan];
+  int arrive[kCenSpan];
+  int queue[2][kCenSpan];
+  int qn[2];
+};
+
+// Centroid of quad node `node`; children inside [lo, hi) are read from the
+// block's shared copy when `local_kids`, all others from global memory.
+__device__ __forceinline__ double2 node_centroid(const TreeArgs &t, int node, int lo, int hi, bool local_kids,
+                                                 const CenSmem &S) {
+  const int p = t.dlt[node];
+  // the same FP64 sums as 0.0 + c0 + c1 + ... with the exact steps
+  // (conversions, the first addition, /2 and /4) in integer arithmetic
+  double cx = 0.0, cy = 0.0;
+  int cnt = 0;
+  if (p >= 64) {
+    // run of identical keys: every point is a child (the reference
+    // recurses without end here; see the oracle's note)
+    const int2 rg = t.range[node];
+    for (int q = rg.x; q <= rg.y; q++) {
+      const float2 v = t.spos[q];
+      cx = cnt ? __dadd_rn(cx, f2d_int(v.x)) : zero_plus(f2d_int(v.x));
+      cy = cnt ? __dadd_rn(cy, f2d_int(v.y)) : zero_plus(f2d_int(v.y));
+      cnt++;
     }
+  } else {
+    const int4 kk = t.qkids[node];
+    const int kids[4] = {kk.x, kk.y, kk.z, kk.w};
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const int ch = kids[c];
+      if (ch == kNoChild) break;
+      double vx, vy;
+      if (ch < 0) {
+        const float2 v = t.spos[~ch];
+        vx = f2d_int(v.x);
+        vy = f2d_int(v.y);
+      } else {
+        double2 v;
+        if (local_kids && ch >= lo && ch < hi) {
+          const int2 cr = t.range[ch];
+          v = (cr.x >= lo && cr.y < hi) ? S.cen[ch - lo] : __ldcg(&t.qcen[ch]);
+        } else {
+          v = __ldcg(&t.qcen[ch]);
+        }
+        vx = v.x;
+        vy = v.y;
+      }
+      cx = c ? __dadd_rn(cx, vx) : zero_plus(vx);
+      cy = c ? __dadd_rn(cy, vy) : zero_plus(vy);
+      cnt++;
+    }
+  }
+  return make_double2(div_count_int(cx, cnt), div_count_int(cy, cnt));
+}
+
+// Arrival at a node that spans blocks; the last arrival computes it and
+// climbs on (bounded by the tree height).  Its children's centroids are read
+// from global memory: every child's writer arrived with release semantics.
+__device__ void climb_spanning(const TreeArgs &t, int node, const CenSmem &S) {
+  while (node >= 0) {
+    const int need = t.qnchild[node];
+    const int up = t.qpar[node];
+    int old;
+    asm volatile("atom.add.acq_rel.gpu.s32 %0, [%1], 1;" : "=r"(old) : "l"(&t.qarrive[node]) : "memory");
+    if (old != need - 1) return;
+    t.qcen[node] = node_centroid(t, node, 0, 0, false, S);
+    node = up;
+  }
+}
+
+__global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  CenSmem &S = *reinterpret_cast<CenSmem *>(smem_raw);
+  if (!block_status_ok(t.st)) return;
+  const int tid = threadIdx.x;
+  const int lo = blockIdx.x * kCenSpan, hi = min(t.n, lo + kCenSpan);
+  auto local = [&](int node) {
+    const int2 rg = t.range[node];
+    return rg.x >= lo && rg.y < hi;
+  };
+  for (int q = tid; q < kCenSpan; q += kCenThreads) S.arrive[q] = 0;
+  if (tid < 2) S.qn[tid] = 0;
+  __syncthreads();
+  // round 0: every point arrives at its quad parent
+  for (int k = lo + tid; k < hi; k += kCenThreads) {
+    const int par = t.qpar[t.n - 1 + k];
+    if (par < 0) continue;
+    if (local(par)) {
+      if (atomicAdd(&S.arrive[par - lo], 1) == t.qnchild[par] - 1) S.queue[0][atomicAdd(&S.qn[0], 1)] = par;
+    } else {
+      climb_spanning(t, par, S);
+    }
+  }
+  __syncthreads();
+  // rounds: the ready local nodes, one per thread (bounded by the depth of
+  // the block's subtrees: every round moves up one node)
+  for (int cur = 0;; cur ^= 1) {
+    const int cnt = S.qn[cur];
+    if (cnt == 0) break;
+    if (tid == 0) S.qn[cur ^ 1] = 0;
+    __syncthreads();
+    for (int q = tid; q < cnt; q += kCenThreads) {
+      const int node = S.queue[cur][q];
+      const double2 c2 = node_centroid(t, node, lo, hi, true, S);
+      S.cen[node - lo] = c2;
+      t.qcen[node] = c2;
+      const int up = t.qpar[node];
+      if (up < 0) continue;
+      if (local(up)) {
+        if (atomicAdd(&S.arrive[up - lo], 1) == t.qnchild[up] - 1) S.queue[cur ^ 1][atomicAdd(&S.qn[cur ^ 1], 1)] = up;
+      } else {
+        climb_spanning(t, up, S);  // releases this node's centroid first
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -638,6 +689,9 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   BL_CUDA(ctx, cudaMalloc(&s.rep, m * sizeof(float2)));
   BL_CUDA(ctx, cudaMalloc(&s.f0, m * sizeof(float4)));
   BL_CUDA(ctx, cudaMalloc(&s.pos_alt, m * sizeof(float2)));
+  // set here, outside any stream capture of the iteration
+  BL_CUDA(ctx, cudaFuncSetAttribute(centroid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sizeof(CenSmem)));
   s.bh_n = n;
   return 0;
 }
@@ -691,7 +745,7 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   t.qarrive = s.qarrive;
   t.st = s.status;
   chain_kernel<<<nblk(n, 256), 256, 0, st>>>(t);
-  centroid_kernel<<<nblk(n, kCenSpan), kCenThreads, 0, st>>>(t);
+  centroid_kernel<<<nblk(n, kCenSpan), kCenThreads, sizeof(CenSmem), st>>>(t);
   ctx->launches += 4;
   if (int rc = scan_exclusive_int(ctx, s.startcnt, s.startbase, n + 1)) return rc;
   LayoutArgs L;

@@ -113,6 +113,36 @@ def test_morton_order_bit_exact(B, gold):
     assert np.array_equal(xy32[perm], z["bh_sorted"])
 
 
+@pytest.mark.parametrize("layout", ["uniform", "clustered", "ties"])
+def test_morton_order_layouts_bit_exact(B, layout):
+    """The stable key sort on uniform points, on a tight cluster stretched by
+    a few far points (most keys share their top bits), and on many equal
+    keys (ties kept in vertex order)."""
+    from batchlayoutcode_gb300 import graphs as G
+    rng = np.random.default_rng(4)
+    n = 60000
+    if layout == "uniform":
+        xy = rng.uniform(-3, 3, (n, 2))
+    elif layout == "clustered":
+        xy = rng.normal(0, 1e-3, (n, 2))
+        xy[:8] = [[-5, -5], [5, 5], [-5, 5], [5, -5], [0, 5], [5, 0], [-5, 0], [0, -5]]
+    else:
+        xy = rng.integers(0, 40, (n, 2)).astype(np.float64) * 0.125
+    g = G.grid_triangulated(200, 300)
+    assert g.n == n
+    with B.Algorithms(g.rowptr, g.colids) as a:
+        a.nCoordinates = xy
+        frame, keys, perm = a.morton_order()
+    xy32 = xy.astype(np.float32).astype(np.float64)
+    oframe, okeys, operm = oracle.morton_sort(xy32)
+    assert np.array_equal(frame, oframe)
+    assert np.array_equal(keys, okeys)
+    assert np.array_equal(perm, operm)
+    if layout == "clustered":  # nearly all keys share a few top digits
+        top = np.bincount((keys >> np.uint64(56)).astype(np.int64), minlength=256)
+        assert np.sort(top)[-4:].sum() >= n - 8
+
+
 def test_quadtree_bit_exact(B, gold):
     _, z = gold
     with make(B, z) as a:
