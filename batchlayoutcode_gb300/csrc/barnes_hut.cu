@@ -351,6 +351,8 @@ __global__ void __launch_bounds__(256) chain_kernel(TreeArgs t) {
       }
       t.qkids[cur] = make_int4(kids[0], kids[1], kids[2], kids[3]);
       t.qnchild[cur] = m;
+    } else {
+      t.qnchild[cur] = 0;  // merged into its parent: not a quad node
     }
     cur = (cur == 0) ? -1 : t.parent[cur];
   }
@@ -363,85 +365,74 @@ __global__ void __launch_bounds__(256) chain_kernel(TreeArgs t) {
 // computed once every child is done.  A block owns kCenSpan consecutive
 // sorted points; a binary node whose range lies inside them has its index
 // there too (a Karras node's index is one of its range ends), so the block
-// keeps those nodes' arrival counters and centroids in shared memory and
-// processes them in rounds: the nodes whose children are all done form a
-// queue, handled one node per thread so that the FP64 work (a small fraction
-// of the FP32 rate on this part, charged per warp instruction) runs in full
-// warps, and a node's last arriving child appends it to the next round's
-// queue.  A node that spans blocks is computed by the thread whose arrival
-// at it (device-scope acquire-release counter) is the last, which climbs on
-// from there: such nodes are few.
-constexpr int kCenThreads = 1024;
-constexpr int kCenSpan = 2048;  // sorted points per block
+// loads those nodes' structure and its points into shared memory with
+// coalesced reads, and processes the nodes in rounds: the nodes whose
+// children are all done form a queue, handled one node per thread so that the
+// FP64 work (a small fraction of the FP32 rate on this part, charged per warp
+// instruction) runs in full warps, and a node's last arriving child appends
+// it to the next round's queue.  A node that spans blocks is computed by the
+// thread whose arrival at it (device-scope acquire-release counter) is the
+// last, which climbs on from there: such nodes are few.
+constexpr int kCenThreads = 512;
+constexpr int kCenSpan = 1024;  // sorted points per block
 
 struct CenSmem {
   double2 cen[kCenSpan];
+  int4 kids[kCenSpan];
+  float2 pts[kCenSpan];
+  int dlt[kCenSpan];
+  int par[kCenSpan];       // quad parent of the local node at this index
+  int leafpar[kCenSpan];   // quad parent of the point at this index
   int arrive[kCenSpan];
   int queue[2][kCenSpan];
+  unsigned short need[kCenSpan];  // children of the local quad node here (<= kCenSpan), 0 if none
   int qn[2];
 };
 
-// Centroid of quad node `node`; children inside [lo, hi) are read from the
-// block's shared copy when `local_kids`, all others from global memory.
-__device__ __forceinline__ double2 node_centroid(const TreeArgs &t, int node, int lo, int hi, bool local_kids,
-                                                 const CenSmem &S) {
-  const int p = t.dlt[node];
-  // the same FP64 sums as 0.0 + c0 + c1 + ... with the exact steps
-  // (conversions, the first addition, /2 and /4) in integer arithmetic
-  double cx = 0.0, cy = 0.0;
-  int cnt = 0;
-  if (p >= 64) {
-    // run of identical keys: every point is a child (the reference
-    // recurses without end here; see the oracle's note)
-    const int2 rg = t.range[node];
-    for (int q = rg.x; q <= rg.y; q++) {
-      const float2 v = t.spos[q];
-      cx = cnt ? __dadd_rn(cx, f2d_int(v.x)) : zero_plus(f2d_int(v.x));
-      cy = cnt ? __dadd_rn(cy, f2d_int(v.y)) : zero_plus(f2d_int(v.y));
-      cnt++;
-    }
-  } else {
-    const int4 kk = t.qkids[node];
-    const int kids[4] = {kk.x, kk.y, kk.z, kk.w};
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-      const int ch = kids[c];
-      if (ch == kNoChild) break;
-      double vx, vy;
-      if (ch < 0) {
-        const float2 v = t.spos[~ch];
-        vx = f2d_int(v.x);
-        vy = f2d_int(v.y);
-      } else {
-        double2 v;
-        if (local_kids && ch >= lo && ch < hi) {
-          const int2 cr = t.range[ch];
-          v = (cr.x >= lo && cr.y < hi) ? S.cen[ch - lo] : __ldcg(&t.qcen[ch]);
-        } else {
-          v = __ldcg(&t.qcen[ch]);
-        }
-        vx = v.x;
-        vy = v.y;
-      }
-      cx = c ? __dadd_rn(cx, vx) : zero_plus(vx);
-      cy = c ? __dadd_rn(cy, vy) : zero_plus(vy);
-      cnt++;
-    }
-  }
-  return make_double2(div_count_int(cx, cnt), div_count_int(cy, cnt));
-}
-
 // Arrival at a node that spans blocks; the last arrival computes it and
-// climbs on (bounded by the tree height).  Its children's centroids are read
-// from global memory: every child's writer arrived with release semantics.
-__device__ void climb_spanning(const TreeArgs &t, int node, const CenSmem &S) {
+// climbs on (bounded by the tree height).  Everything is read from global
+// memory: every child's writer arrived with release semantics.
+__device__ void climb_spanning(const TreeArgs &t, int node) {
   while (node >= 0) {
     const int need = t.qnchild[node];
     const int up = t.qpar[node];
+    const int p = t.dlt[node];
+    const int4 kk = t.qkids[node];
     int old;
     asm volatile("atom.add.acq_rel.gpu.s32 %0, [%1], 1;" : "=r"(old) : "l"(&t.qarrive[node]) : "memory");
     if (old != need - 1) return;
-    t.qcen[node] = node_centroid(t, node, 0, 0, false, S);
+    double cx = 0.0, cy = 0.0;
+    int cnt = 0;
+    if (p >= 64) {
+      const int2 rg = t.range[node];
+      for (int q = rg.x; q <= rg.y; q++) {
+        const float2 v = t.spos[q];
+        cx = cnt ? __dadd_rn(cx, f2d_int(v.x)) : zero_plus(f2d_int(v.x));
+        cy = cnt ? __dadd_rn(cy, f2d_int(v.y)) : zero_plus(f2d_int(v.y));
+        cnt++;
+      }
+    } else {
+      const int kids[4] = {kk.x, kk.y, kk.z, kk.w};
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const int ch = kids[c];
+        if (ch == kNoChild) break;
+        double vx, vy;
+        if (ch < 0) {
+          const float2 v = t.spos[~ch];
+          vx = f2d_int(v.x);
+          vy = f2d_int(v.y);
+        } else {
+          const double2 v = __ldcg(&t.qcen[ch]);
+          vx = v.x;
+          vy = v.y;
+        }
+        cx = c ? __dadd_rn(cx, vx) : zero_plus(vx);
+        cy = c ? __dadd_rn(cy, vy) : zero_plus(vy);
+        cnt++;
+      }
+    }
+    t.qcen[node] = make_double2(div_count_int(cx, cnt), div_count_int(cy, cnt));
     node = up;
   }
 }
@@ -452,21 +443,36 @@ __global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
   if (!block_status_ok(t.st)) return;
   const int tid = threadIdx.x;
   const int lo = blockIdx.x * kCenSpan, hi = min(t.n, lo + kCenSpan);
-  auto local = [&](int node) {
-    const int2 rg = t.range[node];
-    return rg.x >= lo && rg.y < hi;
-  };
-  for (int q = tid; q < kCenSpan; q += kCenThreads) S.arrive[q] = 0;
+  // the block's points and local quad nodes, coalesced
+  for (int j = lo + tid; j < hi; j += kCenThreads) {
+    const int q = j - lo;
+    S.pts[q] = t.spos[j];
+    S.leafpar[q] = t.qpar[t.n - 1 + j];
+    S.arrive[q] = 0;
+    int need = 0;
+    if (j < t.n - 1) {
+      const int m = t.qnchild[j];
+      const int2 rg = t.range[j];
+      if (m > 0 && rg.x >= lo && rg.y < hi) {
+        need = m;
+        S.kids[q] = t.qkids[j];
+        S.dlt[q] = t.dlt[j];
+        S.par[q] = t.qpar[j];
+      }
+    }
+    S.need[q] = (unsigned short)need;
+  }
   if (tid < 2) S.qn[tid] = 0;
   __syncthreads();
+  auto is_local = [&](int node) { return node >= lo && node < hi && S.need[node - lo] != 0; };
   // round 0: every point arrives at its quad parent
   for (int k = lo + tid; k < hi; k += kCenThreads) {
-    const int par = t.qpar[t.n - 1 + k];
+    const int par = S.leafpar[k - lo];
     if (par < 0) continue;
-    if (local(par)) {
-      if (atomicAdd(&S.arrive[par - lo], 1) == t.qnchild[par] - 1) S.queue[0][atomicAdd(&S.qn[0], 1)] = par;
+    if (is_local(par)) {
+      if (atomicAdd(&S.arrive[par - lo], 1) == (int)S.need[par - lo] - 1) S.queue[0][atomicAdd(&S.qn[0], 1)] = par;
     } else {
-      climb_spanning(t, par, S);
+      climb_spanning(t, par);
     }
   }
   __syncthreads();
@@ -479,15 +485,51 @@ __global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
     __syncthreads();
     for (int q = tid; q < cnt; q += kCenThreads) {
       const int node = S.queue[cur][q];
-      const double2 c2 = node_centroid(t, node, lo, hi, true, S);
-      S.cen[node - lo] = c2;
-      t.qcen[node] = c2;
-      const int up = t.qpar[node];
-      if (up < 0) continue;
-      if (local(up)) {
-        if (atomicAdd(&S.arrive[up - lo], 1) == t.qnchild[up] - 1) S.queue[cur ^ 1][atomicAdd(&S.qn[cur ^ 1], 1)] = up;
+      const int ln = node - lo;
+      double cx = 0.0, cy = 0.0;
+      int nc = 0;
+      if (S.dlt[ln] >= 64) {
+        // run of identical keys: every point is a child (the reference
+        // recurses without end here; see the oracle's note)
+        const int2 rg = t.range[node];
+        for (int k = rg.x; k <= rg.y; k++) {
+          const float2 v = S.pts[k - lo];
+          cx = nc ? __dadd_rn(cx, f2d_int(v.x)) : zero_plus(f2d_int(v.x));
+          cy = nc ? __dadd_rn(cy, f2d_int(v.y)) : zero_plus(f2d_int(v.y));
+          nc++;
+        }
       } else {
-        climb_spanning(t, up, S);  // releases this node's centroid first
+        const int4 kk = S.kids[ln];
+        const int kids[4] = {kk.x, kk.y, kk.z, kk.w};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const int ch = kids[c];
+          if (ch == kNoChild) break;
+          double vx, vy;
+          if (ch < 0) {  // a point of this block
+            const float2 v = S.pts[~ch - lo];
+            vx = f2d_int(v.x);
+            vy = f2d_int(v.y);
+          } else {  // a local node, done in an earlier round
+            const double2 v = S.cen[ch - lo];
+            vx = v.x;
+            vy = v.y;
+          }
+          cx = c ? __dadd_rn(cx, vx) : zero_plus(vx);
+          cy = c ? __dadd_rn(cy, vy) : zero_plus(vy);
+          nc++;
+        }
+      }
+      const double2 c2 = make_double2(div_count_int(cx, nc), div_count_int(cy, nc));
+      S.cen[ln] = c2;
+      t.qcen[node] = c2;
+      const int up = S.par[ln];
+      if (up < 0) continue;
+      if (is_local(up)) {
+        if (atomicAdd(&S.arrive[up - lo], 1) == (int)S.need[up - lo] - 1)
+          S.queue[cur ^ 1][atomicAdd(&S.qn[cur ^ 1], 1)] = up;
+      } else {
+        climb_spanning(t, up);  // releases this node's centroid first
       }
     }
     __syncthreads();
