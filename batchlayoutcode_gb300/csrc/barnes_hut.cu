@@ -657,36 +657,87 @@ struct SweepArgs {
 
 constexpr int kSweepThreads = 1024;
 
+// A vertex's data that does not change during the sweep: its slot in the
+// level order, id, iteration-start position, f0 and earlier-batch neighbour
+// range.
+struct SweepVertex {
+  int t, i;
+  float2 pi;
+  float4 f;
+  int e0, e1;
+};
+
+__device__ __forceinline__ void sweep_load(const SweepArgs &a, int t, SweepVertex &v) {
+  v.t = t;
+  v.i = a.order[t];
+  v.pi = a.pold[v.i];
+  v.f = a.f0[v.i];
+  v.e0 = a.early_off[t];
+  v.e1 = a.early_off[t + 1];
+}
+
 // Adds the attraction of the neighbours that moved earlier in this iteration
 // (earlier batches, their new positions) to f0, then the unit-step update
 // (algorithms.cpp:1056-1066).  FP32 terms, float-float sum, FP32 unit vector.
-__device__ __forceinline__ void sweep_vertex(const SweepArgs &a, int t) {
-  const int i = a.order[t];
-  const float2 pi = a.pold[i];
-  const float4 f = a.f0[i];
-  float hx = f.x, hy = f.y, lx = f.z, ly = f.w;
-  const int e1 = a.early_off[t + 1];
-  for (int e = a.early_off[t]; e < e1; e++) bh_attract(__ldcg(&a.pnew[a.early_col[e]]), pi, a.W, hx, lx, hy, ly);
-  const float2 np = bh_step(pi, hx, lx, hy, ly, a.step);
-  a.pnew[i] = np;
+__device__ __forceinline__ void sweep_vertex(const SweepArgs &a, const SweepVertex &v) {
+  float hx = v.f.x, hy = v.f.y, lx = v.f.z, ly = v.f.w;
+  int e = v.e0;
+  // the gathers of up to four moved neighbours are issued together; the
+  // terms are added in neighbour order
+  for (; e + 4 <= v.e1; e += 4) {
+    const int c0 = a.early_col[e], c1 = a.early_col[e + 1], c2 = a.early_col[e + 2], c3 = a.early_col[e + 3];
+    const float2 q0 = __ldcg(&a.pnew[c0]), q1 = __ldcg(&a.pnew[c1]), q2 = __ldcg(&a.pnew[c2]),
+                 q3 = __ldcg(&a.pnew[c3]);
+    bh_attract(q0, v.pi, a.W, hx, lx, hy, ly);
+    bh_attract(q1, v.pi, a.W, hx, lx, hy, ly);
+    bh_attract(q2, v.pi, a.W, hx, lx, hy, ly);
+    bh_attract(q3, v.pi, a.W, hx, lx, hy, ly);
+  }
+  if (e + 2 <= v.e1) {
+    const int c0 = a.early_col[e], c1 = a.early_col[e + 1];
+    const float2 q0 = __ldcg(&a.pnew[c0]), q1 = __ldcg(&a.pnew[c1]);
+    bh_attract(q0, v.pi, a.W, hx, lx, hy, ly);
+    bh_attract(q1, v.pi, a.W, hx, lx, hy, ly);
+    e += 2;
+  }
+  if (e < v.e1) bh_attract(__ldcg(&a.pnew[a.early_col[e]]), v.pi, a.W, hx, lx, hy, ly);
+  const float2 np = bh_step(v.pi, hx, lx, hy, ly, a.step);
+  a.pnew[v.i] = np;
   if (a.write_out) {
     const double fx = (double)hx + (double)lx, fy = (double)hy + (double)ly;
-    a.force[i] = make_double2(fx, fy);
-    a.e[i] = fx * fx + fy * fy;
+    a.force[v.i] = make_double2(fx, fy);
+    a.e[v.i] = fx * fx + fy * fy;
   }
 }
 
 // One cooperative launch for all dependency levels of an iteration; a
-// bounded grid barrier separates the levels.
-__global__ void __launch_bounds__(kSweepThreads, 2) sweep_kernel(SweepArgs a) {
+// bounded grid barrier separates the levels.  Between a thread's arrival at
+// the barrier and its wait, it loads its first vertex of the next level
+// (nothing of it changes during the sweep), so a level after the barrier
+// costs the gathers of the moved neighbours only.
+__global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs a) {
   if (!block_status_ok(a.st)) return;  // every block sees the same value: no barrier is left waiting
   unsigned int epoch = 0;
   const int gsz = gridDim.x * blockDim.x;
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  SweepVertex first;
+  first.t = -1;
+  if (a.levels > 0 && a.level_off[0] + t0 < a.level_off[1]) sweep_load(a, a.level_off[0] + t0, first);
   for (int l = 0; l < a.levels; l++) {
     const int lo = a.level_off[l], hi = a.level_off[l + 1];
-    for (int t = lo + t0; t < hi; t += gsz) sweep_vertex(a, t);
-    if (l + 1 < a.levels && !grid_barrier(a.st, epoch)) return;
+    if (first.t >= 0) sweep_vertex(a, first);
+    for (int t = lo + t0 + gsz; t < hi; t += gsz) {
+      SweepVertex v;
+      sweep_load(a, t, v);
+      sweep_vertex(a, v);
+    }
+    if (l + 1 < a.levels) {
+      grid_arrive(a.st, epoch);
+      first.t = -1;
+      const int nlo = a.level_off[l + 1];
+      if (nlo + t0 < a.level_off[l + 2]) sweep_load(a, nlo + t0, first);
+      if (!grid_wait(a.st, epoch)) return;
+    }
   }
 }
 
