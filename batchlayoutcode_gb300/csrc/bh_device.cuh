@@ -34,6 +34,27 @@ __device__ __forceinline__ u64 spread32(unsigned int v) {
   return x;
 }
 
+// float -> double without the conversion instruction (exact; the bits are
+// rebiased and shifted): normal floats and +-0; subnormal, infinite and NaN
+// floats take the conversion.
+__device__ __forceinline__ double f2d_int(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int e = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  if (e == 0u) {
+    if (u & 0x7fffffu) return (double)f;
+    return __longlong_as_double((long long)sign);
+  }
+  if (e == 0xffu) return (double)f;
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
+// 0.0 + x exactly: x, except that -0 becomes +0.
+__device__ __forceinline__ double zero_plus(double x) {
+  return (__double_as_longlong(x) == (long long)0x8000000000000000ll) ? 0.0 : x;
+}
+
 // Frame (MortonCode.h:42-52) from the ordered-uint bbox {min x, max x, min y,
 // max y}; FP64 like the reference.
 __device__ __forceinline__ void frame_from_bbox(const unsigned int *bbox, double &minX, double &minY,
@@ -48,17 +69,25 @@ __device__ __forceinline__ void frame_from_bbox(const unsigned int *bbox, double
 
 // (uint32)(4294967295.0 * (v - mn) / maxmin), MortonCode.h:62-67, no contraction.
 // The quotient is formed with the reciprocal (one multiply); its error is a
-// few ulp, so unless it lies within 4 ulp of an integer its truncation equals
-// the truncation of the correctly rounded quotient.  Otherwise the exact
-// division decides.
+// couple of ulp, so unless it lies within 8 ulp of an integer its truncation
+// equals the truncation of the correctly rounded quotient.  Otherwise the
+// exact division decides.  The truncation and the distance to the nearest
+// integers are read from the bits of the quotient with integer operations:
+// the FP64 pipe (a small fraction of the FP32 rate on this part) only sees
+// the subtraction and the two products.
 __device__ __forceinline__ unsigned int quantise(float v, double mn, double maxmin, double inv) {
   if (!(maxmin > 0.0)) return 0u;
-  const double a = __dmul_rn(4294967295.0, __dsub_rn((double)v, mn));
+  const double a = __dmul_rn(4294967295.0, __dsub_rn(f2d_int(v), mn));
   const double qf = __dmul_rn(a, inv);
-  const double fl = floor(qf);
-  const double eps = 4.0 * fabs(qf) * 1.1102230246251565e-16 + 1e-300;
-  if (qf - fl > eps && (fl + 1.0) - qf > eps) return __double2uint_rz(fl);
-  return __double2uint_rz(__ddiv_rn(a, maxmin));
+  const unsigned long long b = (unsigned long long)__double_as_longlong(qf);
+  const int e = (int)((b >> 52) & 0x7ffu) - 1023;  // qf in [2^e, 2^(e+1)) when positive
+  if ((b >> 63) == 0ull && e >= 0 && e < 32) {
+    const unsigned long long m = (b & ((1ull << 52) - 1ull)) | (1ull << 52);
+    const int sh = 52 - e;  // fraction bits, 21..52
+    const unsigned long long frac = m & ((1ull << sh) - 1ull);
+    if (frac > 8ull && (1ull << sh) - frac > 8ull) return (unsigned int)(m >> sh);
+  }
+  return __double2uint_rz(__ddiv_rn(a, maxmin));  // near an integer, below 1 or out of range
 }
 
 // 64-bit Morton key, y bit above x bit of every digit (MortonCode.h:83-97).
@@ -97,27 +126,6 @@ __device__ __forceinline__ double div_count_int(double x, int c) {
     if (e > k && e < 0x7ffu) return __longlong_as_double((long long)(b - ((unsigned long long)k << 52)));
   }
   return div_count(x, c);
-}
-
-// float -> double without the conversion instruction (exact; the bits are
-// rebiased and shifted): normal floats and +-0; subnormal, infinite and NaN
-// floats take the conversion.
-__device__ __forceinline__ double f2d_int(float f) {
-  const unsigned int u = __float_as_uint(f);
-  const unsigned int e = (u >> 23) & 0xffu;
-  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
-  if (e == 0u) {
-    if (u & 0x7fffffu) return (double)f;
-    return __longlong_as_double((long long)sign);
-  }
-  if (e == 0xffu) return (double)f;
-  return __longlong_as_double(
-      (long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
-}
-
-// 0.0 + x exactly: x, except that -0 becomes +0.
-__device__ __forceinline__ double zero_plus(double x) {
-  return (__double_as_longlong(x) == (long long)0x8000000000000000ll) ? 0.0 : x;
 }
 
 // Loads of the tree records and positions: through the read-only data cache
