@@ -566,7 +566,7 @@ __global__ void layout_kernel(LayoutArgs L, TreeArgs t) {
     }
     const float2 p = L.spos[i];
     L.nodes[idx] = make_float4(p.x, p.y, 0.0f, __int_as_float(idx + 1));
-    L.nodes_c64[idx] = make_double2((double)p.x, (double)p.y);
+    L.nodes_c64[idx] = make_double2(f2d_int(p.x), f2d_int(p.y));
     L.nodes_lvl[idx] = 255;
   }
   if (i < L.n - 1 && !is_sub(t, i)) {  // quad node = binary internal node i
@@ -583,7 +583,7 @@ __global__ void layout_kernel(LayoutArgs L, TreeArgs t) {
     }
     const double D = ldexp(maxmin, -lvl);
     const double2 c = L.qcen[i];
-    L.nodes[idx] = make_float4((float)c.x, (float)c.y, (float)(D * D), __int_as_float(skip));
+    L.nodes[idx] = make_float4(d2f_int(c.x), d2f_int(c.y), d2f_int(D * D), __int_as_float(skip));
     L.nodes_c64[idx] = c;
     L.nodes_lvl[idx] = (unsigned char)lvl;
   }

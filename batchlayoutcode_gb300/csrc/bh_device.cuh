@@ -50,6 +50,23 @@ __device__ __forceinline__ double f2d_int(float f) {
       (long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
 }
 
+// double -> float rounded to nearest even, with integer operations for the
+// normal range of float (the conversion instruction runs on the FP64 pipe);
+// anything else takes the conversion.
+__device__ __forceinline__ float d2f_int(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ffu) - 1023 + 127;  // float exponent field
+  if (e < 1 || e > 253) return __double2float_rn(x);    // zero, subnormal, near overflow, inf, NaN
+  const unsigned int sign = (unsigned int)(b >> 63) << 31;
+  const unsigned long long man = b & ((1ull << 52) - 1ull);
+  unsigned int m = (unsigned int)(man >> 29);             // 23 bits
+  const unsigned long long rest = man & ((1ull << 29) - 1ull);
+  const unsigned long long half = 1ull << 28;
+  unsigned int bits = sign | ((unsigned int)e << 23) | m;
+  if (rest > half || (rest == half && (m & 1u))) bits += 1u;  // a carry moves into the exponent correctly
+  return __uint_as_float(bits);
+}
+
 // 0.0 + x exactly: x, except that -0 becomes +0.
 __device__ __forceinline__ double zero_plus(double x) {
   return (__double_as_longlong(x) == (long long)0x8000000000000000ll) ? 0.0 : x;
