@@ -8,7 +8,9 @@
 //   1. bbox of the positions; Morton frame {minX, minY, MAXMIN} and 64-bit keys
 //      (y-major interleave of the two 32-bit quantised coordinates, quantised
 //      in FP64 exactly as the reference: (uint32)(4294967295.0*(x-minX)/MAXMIN)).
-//   2. stable LSD radix sort of (key, vertex) pairs, 8 passes of 8 bits.
+//   2. stable LSD radix sort of (key, vertex) pairs on the high 32 bits (4
+//      passes of 8 bits), then each run of equal high halves sorted on its
+//      own (they are rare).
 //   3. binary radix tree over the sorted keys (Karras 2012), then a bottom-up
 //      pass that merges the x-bit level into the y-bit level of the same
 //      digit, giving exactly the reference quadtree without its single-child
@@ -227,6 +229,194 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
         vout[p] = vin[wbase + r * 32 + lane];
       }
     }
+  }
+}
+
+// ---- the low 32 bits: only inside runs of equal high halves ---------------------
+//
+// The four LSD passes on bits 32..63 leave the keys ordered by their high
+// halves and, within a run of equal high halves, by vertex id (the passes are
+// stable and the keys started in vertex order).  A run means two points in
+// the same cell of a 65,536 x 65,536 grid over the frame: rare (a uniform
+// million points give ~100 runs of two).  So each run is finished on its own,
+// by (key, vertex id): runs of up to 32 keys by one thread (insertion sort),
+// longer ones by one block each (bitonic network in shared memory up to
+// kRunCap keys, beyond that stable 8-bit LSD passes through global memory).
+// The result is the stable order of the full 64-bit keys.
+constexpr int kRunShort = 32;
+constexpr int kRunCap = 2048;
+constexpr int kRunThreads = 512;
+
+__device__ __forceinline__ unsigned int hi32(u64 k) { return (unsigned int)(k >> 32); }
+
+// One thread per position; a run's first position sorts a short run or
+// queues a long one (runs[0] = count, then start, length pairs; runs_cap
+// exceeds n / (kRunShort + 1), the most long runs there can be).
+__global__ void run_fix_kernel(u64 *__restrict__ keys, int *__restrict__ vals, int n, int *runs, int runs_cap,
+                               DevStatus *st) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const unsigned int h = hi32(keys[k]);
+  if (k > 0 && hi32(keys[k - 1]) == h) return;        // not a run start
+  if (k + 1 >= n || hi32(keys[k + 1]) != h) return;   // a run of one
+  int len = 2;
+  while (k + len < n && hi32(keys[k + len]) == h && len <= kRunShort) len++;  // bounded scan
+  if (len <= kRunShort) {
+    // insertion sort by (key, vertex id); already in vertex-id order
+    for (int a = k + 1; a < k + len; a++) {
+      const u64 ka = keys[a];
+      const int va = vals[a];
+      int b = a - 1;
+      while (b >= k && (keys[b] > ka || (keys[b] == ka && vals[b] > va))) {
+        keys[b + 1] = keys[b];
+        vals[b + 1] = vals[b];
+        b--;
+      }
+      keys[b + 1] = ka;
+      vals[b + 1] = va;
+    }
+    return;
+  }
+  while (k + len < n && hi32(keys[k + len]) == h) len++;  // the whole run
+  const int slot = atomicAdd(&runs[0], 1);
+  if (slot < runs_cap) {
+    runs[1 + 2 * slot] = k;
+    runs[2 + 2 * slot] = len;
+  } else {
+    dev_record_error(st, DEV_BAD_INDEX);  // cannot happen (see runs_cap)
+  }
+}
+
+struct RunSmem {
+  union {
+    struct {
+      u64 k[kRunCap];
+      int v[kRunCap];
+    } b;
+    struct {
+      unsigned int cnt[kRunThreads / 32][256];
+      unsigned int base[256];
+      unsigned int carry[256];
+      unsigned int tot[256];
+    } c;
+  } u;
+  unsigned int ws[kRunThreads / 32];
+};
+
+// Exclusive scan of x over the first 256 threads; all threads call.
+__device__ __forceinline__ unsigned int run_scan256(unsigned int x, RunSmem &S) {
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  unsigned int inc = x;
+  if (tid < 256) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned int y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    if (lane == 31) S.ws[w] = inc;
+  }
+  __syncthreads();
+  unsigned int pre = 0;
+  if (tid < 256)
+    for (int q = 0; q < w; q++) pre += S.ws[q];
+  __syncthreads();
+  return pre + inc - x;
+}
+
+// One block per queued run (grid-stride over the queue).
+__global__ void __launch_bounds__(kRunThreads) run_sort_kernel(u64 *__restrict__ keys, int *__restrict__ vals,
+                                                               u64 *__restrict__ kalt, int *__restrict__ valt,
+                                                               const int *runs, int runs_cap) {
+  __shared__ RunSmem S;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int count = min(runs[0], runs_cap);
+  for (int r = blockIdx.x; r < count; r += gridDim.x) {
+    const int start = runs[1 + 2 * r], len = runs[2 + 2 * r];
+    if (len <= kRunCap) {
+      int m = 2;
+      while (m < len) m <<= 1;
+      for (int q = tid; q < m; q += kRunThreads) {
+        S.u.b.k[q] = q < len ? keys[start + q] : ~0ull;
+        S.u.b.v[q] = q < len ? vals[start + q] : INT_MAX;
+      }
+      __syncthreads();
+      for (int size = 2; size <= m; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+          for (int i = tid; i < (m >> 1); i += kRunThreads) {
+            const int lo = ((i & ~(stride - 1)) << 1) | (i & (stride - 1));
+            const int hi = lo + stride;
+            const bool up = (lo & size) == 0;
+            const u64 ka = S.u.b.k[lo], kb = S.u.b.k[hi];
+            const int va = S.u.b.v[lo], vb = S.u.b.v[hi];
+            if ((ka > kb || (ka == kb && va > vb)) == up) {
+              S.u.b.k[lo] = kb;
+              S.u.b.k[hi] = ka;
+              S.u.b.v[lo] = vb;
+              S.u.b.v[hi] = va;
+            }
+          }
+          __syncthreads();
+        }
+      }
+      for (int q = tid; q < len; q += kRunThreads) {
+        keys[start + q] = S.u.b.k[q];
+        vals[start + q] = S.u.b.v[q];
+      }
+      __syncthreads();
+      continue;
+    }
+    // a long run: four stable 8-bit passes on the low 32 bits through
+    // global memory (keys <-> the same range of kalt), chunk by chunk
+    const unsigned int lt = (1u << lane) - 1u;
+    for (int pass = 0; pass < 4; pass++) {
+      const u64 *ks = (pass & 1) ? kalt + start : keys + start;
+      const int *vs = (pass & 1) ? valt + start : vals + start;
+      u64 *kd = (pass & 1) ? keys + start : kalt + start;
+      int *vd = (pass & 1) ? vals + start : valt + start;
+      const int shift = 8 * pass;
+      if (tid < 256) S.u.c.carry[tid] = 0;
+      __syncthreads();
+      for (int q = tid; q < len; q += kRunThreads) atomicAdd(&S.u.c.carry[(unsigned int)(ks[q] >> shift) & 255u], 1u);
+      __syncthreads();
+      const unsigned int pre = run_scan256(tid < 256 ? S.u.c.carry[tid] : 0u, S);
+      if (tid < 256) {
+        S.u.c.base[tid] = pre;
+        S.u.c.carry[tid] = 0;
+      }
+      __syncthreads();
+      for (int c0 = 0; c0 < len; c0 += kRunThreads) {  // one key per thread and chunk
+        for (int q = tid; q < (kRunThreads / 32) * 256; q += kRunThreads) (&S.u.c.cnt[0][0])[q] = 0;
+        __syncthreads();
+        const int q = c0 + tid;
+        const bool valid = q < len;
+        const u64 key = valid ? ks[q] : 0ull;
+        const int val = valid ? vs[q] : 0;
+        const unsigned int d = valid ? ((unsigned int)(key >> shift) & 255u) : 256u;
+        const unsigned int peers = __match_any_sync(0xffffffffu, d);
+        const unsigned int rank = __popc(peers & lt);
+        if (d < 256u && lane == __ffs(peers) - 1) S.u.c.cnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (tid < 256) {
+          unsigned int run = 0;
+          for (int w = 0; w < kRunThreads / 32; w++) {
+            const unsigned int c = S.u.c.cnt[w][tid];
+            S.u.c.cnt[w][tid] = run;
+            run += c;
+          }
+          S.u.c.tot[tid] = run;
+        }
+        __syncthreads();
+        if (d < 256u) {
+          const unsigned int p = S.u.c.base[d] + S.u.c.carry[d] + S.u.c.cnt[warp][d] + rank;
+          kd[p] = key;
+          vd[p] = val;
+        }
+        __syncthreads();
+        if (tid < 256) S.u.c.carry[tid] += S.u.c.tot[tid];
+        __syncthreads();
+      }
+    }
+    // four passes end where they started (keys/vals)
   }
 }
 
@@ -754,7 +944,7 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   fr(s.bparent); fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.qkids); fr(s.qpar); fr(s.qnchild);
   fr(s.qarrive); fr(s.qcen);
   fr(s.qbelow); fr(s.startcnt); fr(s.startbase); fr(s.nodes); fr(s.nodes_c64);
-  fr(s.nodes_lvl); fr(s.rep); fr(s.f0); fr(s.pos_alt);
+  fr(s.nodes_lvl); fr(s.rep); fr(s.f0); fr(s.pos_alt); fr(s.runs);
   const size_t nb = (n + kRsTile - 1) / kRsTile;
   s.hist_entries = 256 * std::max<size_t>(nb, 1) + 256;
   const size_t m = std::max<size_t>(n, 2);
@@ -782,6 +972,8 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   BL_CUDA(ctx, cudaMalloc(&s.rep, m * sizeof(float2)));
   BL_CUDA(ctx, cudaMalloc(&s.f0, m * sizeof(float4)));
   BL_CUDA(ctx, cudaMalloc(&s.pos_alt, m * sizeof(float2)));
+  s.runs_cap = (int)(m / (kRunShort + 1) + 1);  // runs longer than kRunShort: at most n / (kRunShort + 1)
+  BL_CUDA(ctx, cudaMalloc(&s.runs, (2 * (size_t)s.runs_cap + 1) * sizeof(int)));
   // set here, outside any stream capture of the iteration
   BL_CUDA(ctx, cudaFuncSetAttribute(centroid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)sizeof(CenSmem)));
@@ -808,7 +1000,8 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   // hist layout: [256 digits x ntiles counts][256 digit-row totals]
   unsigned int *digit_off = s.hist + (size_t)256 * nb;
   bl_time_begin(ctx, "radix_sort");
-  for (int pass = 0; pass < 8; pass++) {
+  // bits 32..63 by four LSD passes, then the runs of equal high halves
+  for (int pass = 4; pass < 8; pass++) {
     rs_count_kernel<<<nb, kRsThreads, 0, st>>>(kin, n, 8 * pass, nb, s.hist);
     rs_rowscan_kernel<<<256, 256, 0, st>>>(s.hist, nb, digit_off);
     rs_scatter_kernel<<<nb, kRsThreads, 0, st>>>(kin, vin, kout, vout, n, 8 * pass, nb, s.hist, digit_off);
@@ -816,8 +1009,12 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
     std::swap(vin, vout);
     ctx->launches += 3;
   }
+  // 4 passes: the data is back in keys/perm
+  BL_CUDA(ctx, cudaMemsetAsync(s.runs, 0, sizeof(int), st));
+  run_fix_kernel<<<nblk(n, 256), 256, 0, st>>>(s.keys, s.perm, n, s.runs, s.runs_cap, s.status);
+  run_sort_kernel<<<ctx->num_sms, kRunThreads, 0, st>>>(s.keys, s.perm, s.keys_alt, s.perm_alt, s.runs, s.runs_cap);
+  ctx->launches += 2;
   bl_time_end(ctx, "radix_sort");
-  // 8 passes: sorted data is back in keys/perm
   gather_kernel<<<nblk(n, 256), 256, 0, st>>>(pos, s.perm, n, s.spos);
   radix_tree_kernel<<<nblk(n - 1, 256), 256, 0, st>>>(s.keys, n, s.bchild, s.brange, s.bdelta, s.bparent);
   BL_CUDA(ctx, cudaMemsetAsync(s.qarrive, 0, (size_t)n * sizeof(int), st));

@@ -192,6 +192,8 @@ struct Scratch {
   unsigned long long *keys = nullptr, *keys_alt = nullptr;
   int *perm = nullptr, *perm_alt = nullptr;
   unsigned int *hist = nullptr;  // radix histograms / offsets
+  int *runs = nullptr;           // runs of equal high key halves: count, (start, length) pairs, overflow
+  int runs_cap = 0;
   size_t hist_entries = 0;
   unsigned int *bbox = nullptr;  // 4 ordered-uint encoded floats
   double *frame = nullptr;       // minX, minY, MAXMIN

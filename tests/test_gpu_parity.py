@@ -113,11 +113,12 @@ def test_morton_order_bit_exact(B, gold):
     assert np.array_equal(xy32[perm], z["bh_sorted"])
 
 
-@pytest.mark.parametrize("layout", ["uniform", "clustered", "ties"])
+@pytest.mark.parametrize("layout", ["uniform", "clustered", "ties", "tight"])
 def test_morton_order_layouts_bit_exact(B, layout):
-    """The stable key sort on uniform points, on a tight cluster stretched by
-    a few far points (most keys share their top bits), and on many equal
-    keys (ties kept in vertex order)."""
+    """The stable key sort on uniform points, on a cluster stretched by a few
+    far points (runs of keys sharing their high halves), on many equal keys
+    (ties kept in vertex order), and on 20,000 points inside one cell of the
+    65,536^2 grid (one long run sorted through global memory)."""
     from batchlayoutcode_gb300 import graphs as G
     rng = np.random.default_rng(4)
     n = 60000
@@ -126,8 +127,11 @@ def test_morton_order_layouts_bit_exact(B, layout):
     elif layout == "clustered":
         xy = rng.normal(0, 1e-3, (n, 2))
         xy[:8] = [[-5, -5], [5, 5], [-5, 5], [5, -5], [0, 5], [5, 0], [-5, 0], [0, -5]]
-    else:
+    elif layout == "ties":
         xy = rng.integers(0, 40, (n, 2)).astype(np.float64) * 0.125
+    else:
+        xy = rng.uniform(-3, 3, (n, 2))
+        xy[:20000] = 1.0 + rng.uniform(0, 1e-6, (20000, 2))
     g = G.grid_triangulated(200, 300)
     assert g.n == n
     with B.Algorithms(g.rowptr, g.colids) as a:
