@@ -686,7 +686,8 @@ def main():
             "config": {"workload": f"{args.workload}: {w['desc']}", "vertices": g.n, "edges": g.nnz // 2,
                        "step": (f"{ips} layout iterations" if ips > 1 else "one layout iteration") +
                                " over the whole graph" +
-                               (" (replay of the captured iteration, a CUDA graph of its 45 launches)" if graph else ""),
+                               (f" (replay of the captured iteration, a CUDA graph of its {launches // args.steps} "
+                                "kernel launches)" if graph else ""),
                        "l2": "flushed before every timed step (256 MB write)",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
