@@ -803,6 +803,7 @@ struct TraverseArgs {
 };
 
 
+template <bool kStats>
 __global__ void __launch_bounds__(256) traverse_kernel(TraverseArgs a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (!block_status_ok(a.st)) return;  // the tree of this iteration is not valid
@@ -815,16 +816,20 @@ __global__ void __launch_bounds__(256) traverse_kernel(TraverseArgs a) {
     total = 0;
   }
   unsigned int visits = 0, exact = 0;
-  const float2 rep = bh_repulsion<true>(a.nodes, a.nodes_c64, a.nodes_lvl, a.frame[2], a.theta2, a.theta, total, q, a.st,
-                                  visits, exact);
+  const float2 rep = bh_repulsion<true, kStats>(a.nodes, a.nodes_c64, a.nodes_lvl, a.frame[2], a.theta2, a.theta,
+                                                total, q, visits, exact);
   const int v = a.perm[k];
   a.rep[v] = rep;
   // FR attraction (algorithms.cpp:1056-1058) of the neighbours that have not
   // moved before v in this iteration
   if (a.f0) a.f0[v] = bh_unmoved_attraction(v, rep, a.rowptr, a.colids, a.pold, a.batch, a.W);
-  if (a.stats) {
-    atomicAdd(&a.stats[0], (unsigned long long)visits);
-    if (exact) atomicAdd(&a.stats[1], (unsigned long long)exact);
+  if (kStats) {  // one atomic per group of converged lanes, not per thread
+    const unsigned int m = __activemask();
+    const unsigned int sv = __reduce_add_sync(m, visits), se = __reduce_add_sync(m, exact);
+    if ((threadIdx.x & 31u) == (unsigned int)(__ffs(m) - 1)) {
+      atomicAdd(&a.stats[0], (unsigned long long)sv);
+      if (se) atomicAdd(&a.stats[1], (unsigned long long)se);
+    }
   }
 }
 
@@ -1087,7 +1092,8 @@ int bh_traverse(bl_ctx *ctx, double theta, bool want_stats, int batch) {
   a.W = (float)ctx->weight;
   if (want_stats) BL_CUDA(ctx, cudaMemsetAsync(s.stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
   bl_time_begin(ctx, "traverse_kernel");
-  traverse_kernel<<<nblk(n, 256), 256, 0, ctx->stream>>>(a);
+  if (want_stats) traverse_kernel<true><<<nblk(n, 256), 256, 0, ctx->stream>>>(a);
+  else traverse_kernel<false><<<nblk(n, 256), 256, 0, ctx->stream>>>(a);
   bl_time_end(ctx, "traverse_kernel");
   ctx->launches++;
   BL_CUDA(ctx, cudaGetLastError());

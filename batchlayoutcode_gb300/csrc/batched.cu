@@ -575,8 +575,8 @@ __device__ void layout_bh(const BatchedArgs &a, int g, BhShared &S, double *red)
       }
       unsigned int visits = 0, exact = 0;
       for (int k = tid; k < n; k += kBThreads) {
-        const float2 rep = bh_repulsion<false>(nodes, c64, nlvl, maxmin, a.theta2, a.theta, total, spos[k], a.st, visits,
-                                        exact);
+        const float2 rep = bh_repulsion<false>(nodes, c64, nlvl, maxmin, a.theta2, a.theta, total, spos[k], visits,
+                                               exact);
         const int v = vin[k];
         f0[v] = bh_unmoved_attraction(v, rep, rp, ci, pos, a.batch, a.W);
       }

@@ -170,12 +170,21 @@ static __device__ __noinline__ bool open_test_fp64(const double2 *c64, const uns
 // (BarnesHut.h:69-86).  The opening test D/dist < theta is evaluated in FP32
 // and re-evaluated in FP64 when the FP32 margin is within its error bound, so
 // every decision equals the reference's FP64 decision.  A leaf at q itself
-// adds nothing (its vector is zero).
-template <bool kRO>
+// adds nothing (its vector is zero).  The step to the next record is
+// max(skip, i + 1) on acceptance, so the walk ends after at most `total`
+// records whatever the records hold (the layout checks every skip link).
+// kStats counts record visits and FP64 decisions.
+template <bool kRO, bool kStats = false>
 __device__ __forceinline__ float2 bh_repulsion(const float4 *nodes, const double2 *c64, const unsigned char *lvl,
                                                double maxmin, float theta2, double theta, int total, float2 q,
-                                               DevStatus *st, unsigned int &visits, unsigned int &exact) {
-  const float qm = fabsf(q.x) + fabsf(q.y);
+                                               unsigned int &visits, unsigned int &exact) {
+  // error bound of the FP32 comparison |theta^2 d^2 - D^2|, with a wide
+  // safety factor: 2^-20 (theta^2 d^2 + D^2) for the centroid, theta^2 and
+  // D^2 roundings and the products, plus theta^2 2^-21 s (|qx| + |qy| + |x| +
+  // |y|) <= theta^2 2^-21 s (2 (|qx| + |qy|) + s), s = |dx| + |dy|, for the
+  // rounding of the coordinates and of their differences
+  const float ta = theta2 * 4.7683716e-07f * 1.001f;
+  const float tq = ta * 2.f * (fabsf(q.x) + fabsf(q.y));
   float fx = 0.f, fy = 0.f;
   int i = 0;
   while (i < total) {
@@ -184,30 +193,19 @@ __device__ __forceinline__ float2 bh_repulsion(const float4 *nodes, const double
     const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
     const float lhs = theta2 * d2;
     bool accept = nd.z < lhs;
-    if (nd.z > 0.f) {
-      // error bound of the FP32 comparison (centroid rounding, subtraction,
-      // squares, theta^2 and D^2 rounding), with a wide safety factor
-      const float tol = 9.5367432e-07f * (lhs + nd.z) +
-                        theta2 * 4.7683716e-07f * (fabsf(dx) + fabsf(dy)) * (qm + fabsf(nd.x) + fabsf(nd.y));
-      if (fabsf(lhs - nd.z) <= tol) {
-        accept = open_test_fp64<kRO>(c64, lvl, maxmin, theta, i, q.x, q.y);
-        exact++;
-      }
+    const float sd = fabsf(dx) + fabsf(dy);
+    const float tol = fmaf(sd, fmaf(ta, sd, tq), 9.5367432e-07f * (lhs + nd.z));
+    if (fabsf(lhs - nd.z) <= tol && nd.z > 0.f) {
+      accept = open_test_fp64<kRO>(c64, lvl, maxmin, theta, i, q.x, q.y);
+      if (kStats) exact++;
     }
-    visits++;
+    if (kStats) visits++;
+    const float r = rsqrt_approx(d2);
     if (accept) {
-      const float r = rsqrt_approx(d2);
       fx = fmaf(dx, r, fx);
       fy = fmaf(dy, r, fy);
-      const int nxt = __float_as_int(nd.w);
-      if (nxt <= i) {  // a skip link always moves forward; stop on a corrupt one
-        dev_record_error(st, DEV_BAD_INDEX);
-        break;
-      }
-      i = nxt;
-    } else {
-      i++;
     }
+    i = accept ? max(__float_as_int(nd.w), i + 1) : i + 1;
   }
   return make_float2(fx, fy);
 }
