@@ -304,7 +304,7 @@ bl_ctx *bl_algorithms_create(int device, int n, long long nnz, const int *rowptr
   if ((e = cudaMalloc(&ctx->s.energy_parts, 1024 * sizeof(double))) != cudaSuccess) return bad(e, "cudaMalloc");
   if ((e = cudaMalloc(&ctx->s.energy, 16 * sizeof(double))) != cudaSuccess) return bad(e, "cudaMalloc");
   if ((e = cudaMalloc(&ctx->s.status, sizeof(DevStatus))) != cudaSuccess) return bad(e, "cudaMalloc");
-  if ((e = cudaMalloc(&ctx->s.bbox, 4 * sizeof(unsigned int))) != cudaSuccess) return bad(e, "cudaMalloc");
+  if ((e = cudaMalloc(&ctx->s.bbox, 8 * sizeof(unsigned int))) != cudaSuccess) return bad(e, "cudaMalloc");
   if ((e = cudaMalloc(&ctx->s.frame, 4 * sizeof(double))) != cudaSuccess) return bad(e, "cudaMalloc");
   if ((e = cudaMalloc(&ctx->s.stats, 2 * sizeof(unsigned long long))) != cudaSuccess) return bad(e, "cudaMalloc");
   cudaMemset(ctx->pos, 0, m * sizeof(float2));

@@ -42,57 +42,6 @@ namespace bl {
 namespace {
 
 
-__global__ void bbox_init_kernel(unsigned int *bbox) {
-  if (threadIdx.x == 0) {
-    bbox[0] = 0xffffffffu;  // min x
-    bbox[1] = 0u;           // max x
-    bbox[2] = 0xffffffffu;  // min y
-    bbox[3] = 0u;           // max y
-  }
-}
-
-__global__ void bbox_kernel(const float2 *__restrict__ pos, int n, unsigned int *bbox) {
-  unsigned int mnx = 0xffffffffu, mxx = 0u, mny = 0xffffffffu, mxy = 0u;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float2 p = pos[i];
-    const unsigned int ux = f2ord(p.x), uy = f2ord(p.y);
-    mnx = min(mnx, ux); mxx = max(mxx, ux);
-    mny = min(mny, uy); mxy = max(mxy, uy);
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    mnx = min(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
-    mxx = max(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
-    mny = min(mny, __shfl_xor_sync(0xffffffffu, mny, o));
-    mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicMin(&bbox[0], mnx);
-    atomicMax(&bbox[1], mxx);
-    atomicMin(&bbox[2], mny);
-    atomicMax(&bbox[3], mxy);
-  }
-}
-
-
-__global__ void frame_kernel(const unsigned int *bbox, double *frame) {
-  if (threadIdx.x != 0) return;
-  double minX, minY, maxmin;
-  frame_from_bbox(bbox, minX, minY, maxmin);
-  frame[0] = minX;
-  frame[1] = minY;
-  frame[2] = maxmin;
-  frame[3] = (maxmin > 0.0) ? 1.0 / maxmin : 0.0;
-}
-
-__global__ void morton_kernel(const float2 *__restrict__ pos, int n, u64 *keys, int *vals,
-                              const double *__restrict__ frame) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double minX = frame[0], minY = frame[1], maxmin = frame[2], inv = frame[3];
-  keys[i] = morton_key(pos[i], minX, minY, maxmin, inv);
-  vals[i] = i;
-}
-
 // ---- stable LSD radix sort, 8-bit digits ------------------------------------
 //
 // Each digit pass is three kernels without any inter-block waiting: the tile
@@ -229,6 +178,116 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
         vout[p] = vin[wbase + r * 32 + lane];
       }
     }
+  }
+}
+
+// ---- frame and keys: one cooperative launch ---------------------------------
+//
+// Bounding box of the positions (MortonCode.h:42-58), the FP64 frame
+// {minX, minY, MAXMIN, 1/MAXMIN} and the 64-bit Morton key of every point,
+// together with the tile digit counts of the first sort pass (bits
+// shift..shift+7), so that pass starts at its row scan.  Block b handles
+// sort tiles b, b + grid, ...; one grid barrier separates the box from the
+// keys.  box[0..3] = {min x, ~max x, min y, ~max y} in the order-preserving
+// integer form of the floats and box[4] the arrivals, all reset to
+// 0xffffffff before the launch: every slot only decreases.
+__global__ void __launch_bounds__(kRsThreads, 8) frame_keys_kernel(const float2 *__restrict__ pos, int n, int ntiles,
+                                                                unsigned int *box, double *frame, u64 *keys,
+                                                                int *vals, int shift, unsigned int *hist,
+                                                                DevStatus *st) {
+  __shared__ unsigned int s_box[kRsWarps][4];
+  __shared__ unsigned int cnt[kRsWarps][256];
+  __shared__ double s_frame[4];
+  __shared__ unsigned int s_ok;
+  if (!block_status_ok(st)) return;  // every block sees the same value: no barrier is left waiting
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  unsigned int mnx = 0xffffffffu, mxx = 0u, mny = 0xffffffffu, mxy = 0u;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+#pragma unroll
+    for (int r = 0; r < kRsItems; r++) {
+      const int idx = tile * kRsTile + r * kRsThreads + tid;
+      if (idx < n) {
+        const float2 p = pos[idx];
+        const unsigned int ux = f2ord(p.x), uy = f2ord(p.y);
+        mnx = min(mnx, ux); mxx = max(mxx, ux);
+        mny = min(mny, uy); mxy = max(mxy, uy);
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mnx = min(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+    mxx = max(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+    mny = min(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+    mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+  }
+  if (lane == 0) {
+    s_box[warp][0] = mnx;
+    s_box[warp][1] = ~mxx;
+    s_box[warp][2] = mny;
+    s_box[warp][3] = ~mxy;
+  }
+  __syncthreads();
+  if (tid < 4) {
+    unsigned int v = 0xffffffffu;
+#pragma unroll
+    for (int w = 0; w < kRsWarps; w++) v = min(v, s_box[w][tid]);
+    atomicMin(&box[tid], v);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    atomicSub(&box[4], 1u);
+    const unsigned int target = 0xffffffffu - gridDim.x;  // every block arrived
+    const unsigned long long t0 = dev_globaltimer();
+    unsigned int ok = 1, polls = 0;
+    while (ld_acquire_gpu(&box[4]) > target) {
+      if ((++polls & 127u) == 0u && dev_globaltimer() - t0 > kBarrierTimeoutNs) {
+        dev_record_error(st, DEV_TIMEOUT_GRID_BARRIER);
+        ok = 0;
+        break;
+      }
+    }
+    if (ok) {
+      unsigned int bb[4];
+      bb[0] = ld_volatile_u32(&box[0]);
+      bb[1] = ~ld_volatile_u32(&box[1]);
+      bb[2] = ld_volatile_u32(&box[2]);
+      bb[3] = ~ld_volatile_u32(&box[3]);
+      double minX, minY, maxmin;
+      frame_from_bbox(bb, minX, minY, maxmin);
+      s_frame[0] = minX;
+      s_frame[1] = minY;
+      s_frame[2] = maxmin;
+      s_frame[3] = (maxmin > 0.0) ? 1.0 / maxmin : 0.0;
+      if (blockIdx.x == 0) {
+        for (int k = 0; k < 4; k++) frame[k] = s_frame[k];
+      }
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  if (!s_ok) return;
+  const double minX = s_frame[0], minY = s_frame[1], maxmin = s_frame[2], inv = s_frame[3];
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+#pragma unroll
+    for (int w = 0; w < kRsWarps; w++) cnt[w][tid] = 0;
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kRsItems; r++) {
+      const int idx = tile * kRsTile + r * kRsThreads + tid;
+      if (idx < n) {
+        const u64 key = morton_key(pos[idx], minX, minY, maxmin, inv);
+        keys[idx] = key;
+        vals[idx] = idx;
+        atomicAdd(&cnt[warp][(unsigned int)(key >> shift) & 255u], 1u);
+      }
+    }
+    __syncthreads();
+    unsigned int tot = 0;
+#pragma unroll
+    for (int w = 0; w < kRsWarps; w++) tot += cnt[w][tid];
+    hist[(size_t)tid * ntiles + tile] = tot;
+    __syncthreads();
   }
 }
 
@@ -979,6 +1038,10 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   BL_CUDA(ctx, cudaMalloc(&s.pos_alt, m * sizeof(float2)));
   s.runs_cap = (int)(m / (kRunShort + 1) + 1);  // runs longer than kRunShort: at most n / (kRunShort + 1)
   BL_CUDA(ctx, cudaMalloc(&s.runs, (2 * (size_t)s.runs_cap + 1) * sizeof(int)));
+  int occ = 0;
+  BL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, frame_keys_kernel, kRsThreads, 0));
+  if (occ < 1) return bl_fail(ctx, -5, "frame/key kernel cannot be resident");
+  s.fk_grid = ctx->num_sms * occ;
   // set here, outside any stream capture of the iteration
   BL_CUDA(ctx, cudaFuncSetAttribute(centroid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)sizeof(CenSmem)));
@@ -994,34 +1057,51 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   Scratch &s = ctx->s;
   cudaStream_t st = ctx->stream;
   if (n < 2) return 0;
-  bbox_init_kernel<<<1, 32, 0, st>>>(s.bbox);
-  bbox_kernel<<<std::min(nblk(n, 256), ctx->num_sms * 4), 256, 0, st>>>(pos, n, s.bbox);
-  frame_kernel<<<1, 32, 0, st>>>(s.bbox, s.frame);
-  morton_kernel<<<nblk(n, 256), 256, 0, st>>>(pos, n, s.keys, s.perm, s.frame);
-  ctx->launches += 4;
   const int nb = nblk(n, kRsTile);
   unsigned long long *kin = s.keys, *kout = s.keys_alt;
   int *vin = s.perm, *vout = s.perm_alt;
   // hist layout: [256 digits x ntiles counts][256 digit-row totals]
   unsigned int *digit_off = s.hist + (size_t)256 * nb;
+  bl_time_begin(ctx, "frame_morton");
+  // box and barrier slots to 0xffffffff; then the frame, the keys and the
+  // digit counts of the first pass (bits 32..39) in one cooperative launch
+  BL_CUDA(ctx, cudaMemsetAsync(s.bbox, 0xff, 5 * sizeof(unsigned int), st));
+  {
+    const int grid = std::min(nb, s.fk_grid);
+    int shift = 32;
+    int nn = n;
+    int ntiles = nb;
+    void *args[] = {(void *)&pos, &nn, &ntiles, &s.bbox, &s.frame, &s.keys, &s.perm, &shift, &s.hist, &s.status};
+    BL_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)frame_keys_kernel, dim3(grid), dim3(kRsThreads), args, 0,
+                                             st));
+    ctx->launches++;
+  }
+  bl_time_end(ctx, "frame_morton");
   bl_time_begin(ctx, "radix_sort");
+  bl_time_begin(ctx, "lsd_passes");
   // bits 32..63 by four LSD passes, then the runs of equal high halves
   for (int pass = 4; pass < 8; pass++) {
-    rs_count_kernel<<<nb, kRsThreads, 0, st>>>(kin, n, 8 * pass, nb, s.hist);
+    if (pass > 4) {  // the first pass's counts come with the keys
+      rs_count_kernel<<<nb, kRsThreads, 0, st>>>(kin, n, 8 * pass, nb, s.hist);
+      ctx->launches++;
+    }
     rs_rowscan_kernel<<<256, 256, 0, st>>>(s.hist, nb, digit_off);
     rs_scatter_kernel<<<nb, kRsThreads, 0, st>>>(kin, vin, kout, vout, n, 8 * pass, nb, s.hist, digit_off);
     std::swap(kin, kout);
     std::swap(vin, vout);
-    ctx->launches += 3;
+    ctx->launches += 2;
   }
+  bl_time_end(ctx, "lsd_passes");
   // 4 passes: the data is back in keys/perm
   BL_CUDA(ctx, cudaMemsetAsync(s.runs, 0, sizeof(int), st));
   run_fix_kernel<<<nblk(n, 256), 256, 0, st>>>(s.keys, s.perm, n, s.runs, s.runs_cap, s.status);
   run_sort_kernel<<<ctx->num_sms, kRunThreads, 0, st>>>(s.keys, s.perm, s.keys_alt, s.perm_alt, s.runs, s.runs_cap);
   ctx->launches += 2;
   bl_time_end(ctx, "radix_sort");
+  bl_time_begin(ctx, "gather_tree");
   gather_kernel<<<nblk(n, 256), 256, 0, st>>>(pos, s.perm, n, s.spos);
   radix_tree_kernel<<<nblk(n - 1, 256), 256, 0, st>>>(s.keys, n, s.bchild, s.brange, s.bdelta, s.bparent);
+  bl_time_end(ctx, "gather_tree");
   BL_CUDA(ctx, cudaMemsetAsync(s.qarrive, 0, (size_t)n * sizeof(int), st));
   BL_CUDA(ctx, cudaMemsetAsync(s.startcnt + n, 0, sizeof(int), st));
   TreeArgs t;
@@ -1039,9 +1119,14 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   t.qnchild = s.qnchild;
   t.qarrive = s.qarrive;
   t.st = s.status;
+  bl_time_begin(ctx, "chain_kernel");
   chain_kernel<<<nblk(n, 256), 256, 0, st>>>(t);
+  bl_time_end(ctx, "chain_kernel");
+  bl_time_begin(ctx, "centroid_kernel");
   centroid_kernel<<<nblk(n, kCenSpan), kCenThreads, sizeof(CenSmem), st>>>(t);
+  bl_time_end(ctx, "centroid_kernel");
   ctx->launches += 4;
+  bl_time_begin(ctx, "scan_layout");
   if (int rc = scan_exclusive_int(ctx, s.startcnt, s.startbase, n + 1)) return rc;
   LayoutArgs L;
   L.n = n;
@@ -1059,6 +1144,7 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   L.nodes_lvl = s.nodes_lvl;
   L.st = s.status;
   layout_kernel<<<nblk(n, 256), 256, 0, st>>>(L, t);
+  bl_time_end(ctx, "scan_layout");
   ctx->launches++;
   BL_CUDA(ctx, cudaGetLastError());
   return 0;

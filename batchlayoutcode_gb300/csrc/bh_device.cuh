@@ -165,6 +165,42 @@ static __device__ __noinline__ bool open_test_fp64(const double2 *c64, const uns
   return __ddiv_rn(D, dist) < theta;
 }
 
+// Error-bound constants of bh_walk_step for a query q.  The bound of the FP32
+// comparison |theta^2 d^2 - D^2|, with a wide safety factor, is 2^-20
+// (theta^2 d^2 + D^2) for the centroid, theta^2 and D^2 roundings and the
+// products, plus theta^2 2^-21 s (|qx| + |qy| + |x| + |y|) <= theta^2 2^-21 s
+// (2 (|qx| + |qy|) + s), s = |dx| + |dy|, for the rounding of the coordinates
+// and of their differences.
+__device__ __forceinline__ float bh_tol_a(float theta2) { return theta2 * 4.7683716e-07f * 1.001f; }
+__device__ __forceinline__ float bh_tol_q(float ta, float2 q) { return ta * 2.f * (fabsf(q.x) + fabsf(q.y)); }
+
+// One record of the walk: the opening test on record i, the accepted
+// record's unit vector added to (fx, fy), and the next record.
+template <bool kRO, bool kStats>
+__device__ __forceinline__ void bh_walk_step(const float4 *nodes, const double2 *c64, const unsigned char *lvl,
+                                             double maxmin, float theta2, double theta, float ta, float tq, float2 q,
+                                             int &i, float &fx, float &fy, unsigned int &visits,
+                                             unsigned int &exact) {
+  const float4 nd = ldx<kRO>(&nodes[i]);
+  const float dx = nd.x - q.x, dy = nd.y - q.y;
+  const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
+  const float lhs = theta2 * d2;
+  bool accept = nd.z < lhs;
+  const float sd = fabsf(dx) + fabsf(dy);
+  const float tol = fmaf(sd, fmaf(ta, sd, tq), 9.5367432e-07f * (lhs + nd.z));
+  if (fabsf(lhs - nd.z) <= tol && nd.z > 0.f) {
+    accept = open_test_fp64<kRO>(c64, lvl, maxmin, theta, i, q.x, q.y);
+    if (kStats) exact++;
+  }
+  if (kStats) visits++;
+  const float r = rsqrt_approx(d2);
+  if (accept) {
+    fx = fmaf(dx, r, fx);
+    fy = fmaf(dy, r, fy);
+  }
+  i = accept ? max(__float_as_int(nd.w), i + 1) : i + 1;
+}
+
 // Stackless walk of the pre-order records {x, y, D^2, skip} (record 0 is the
 // root, its skip link is the number of records): repulsion on q
 // (BarnesHut.h:69-86).  The opening test D/dist < theta is evaluated in FP32
@@ -178,35 +214,10 @@ template <bool kRO, bool kStats = false>
 __device__ __forceinline__ float2 bh_repulsion(const float4 *nodes, const double2 *c64, const unsigned char *lvl,
                                                double maxmin, float theta2, double theta, int total, float2 q,
                                                unsigned int &visits, unsigned int &exact) {
-  // error bound of the FP32 comparison |theta^2 d^2 - D^2|, with a wide
-  // safety factor: 2^-20 (theta^2 d^2 + D^2) for the centroid, theta^2 and
-  // D^2 roundings and the products, plus theta^2 2^-21 s (|qx| + |qy| + |x| +
-  // |y|) <= theta^2 2^-21 s (2 (|qx| + |qy|) + s), s = |dx| + |dy|, for the
-  // rounding of the coordinates and of their differences
-  const float ta = theta2 * 4.7683716e-07f * 1.001f;
-  const float tq = ta * 2.f * (fabsf(q.x) + fabsf(q.y));
+  const float ta = bh_tol_a(theta2), tq = bh_tol_q(ta, q);
   float fx = 0.f, fy = 0.f;
   int i = 0;
-  while (i < total) {
-    const float4 nd = ldx<kRO>(&nodes[i]);
-    const float dx = nd.x - q.x, dy = nd.y - q.y;
-    const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
-    const float lhs = theta2 * d2;
-    bool accept = nd.z < lhs;
-    const float sd = fabsf(dx) + fabsf(dy);
-    const float tol = fmaf(sd, fmaf(ta, sd, tq), 9.5367432e-07f * (lhs + nd.z));
-    if (fabsf(lhs - nd.z) <= tol && nd.z > 0.f) {
-      accept = open_test_fp64<kRO>(c64, lvl, maxmin, theta, i, q.x, q.y);
-      if (kStats) exact++;
-    }
-    if (kStats) visits++;
-    const float r = rsqrt_approx(d2);
-    if (accept) {
-      fx = fmaf(dx, r, fx);
-      fy = fmaf(dy, r, fy);
-    }
-    i = accept ? max(__float_as_int(nd.w), i + 1) : i + 1;
-  }
+  while (i < total) bh_walk_step<kRO, kStats>(nodes, c64, lvl, maxmin, theta2, theta, ta, tq, q, i, fx, fy, visits, exact);
   return make_float2(fx, fy);
 }
 

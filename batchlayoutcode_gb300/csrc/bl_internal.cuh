@@ -192,10 +192,11 @@ struct Scratch {
   unsigned long long *keys = nullptr, *keys_alt = nullptr;
   int *perm = nullptr, *perm_alt = nullptr;
   unsigned int *hist = nullptr;  // radix histograms / offsets
+  int fk_grid = 0;               // resident blocks of the frame/key kernel
   int *runs = nullptr;           // runs of equal high key halves: count, (start, length) pairs, overflow
   int runs_cap = 0;
   size_t hist_entries = 0;
-  unsigned int *bbox = nullptr;  // 4 ordered-uint encoded floats
+  unsigned int *bbox = nullptr;  // frame/key kernel: box (ordered-uint floats) and arrivals
   double *frame = nullptr;       // minX, minY, MAXMIN
   float2 *spos = nullptr;        // positions in Morton order
   int *bparent = nullptr;        // binary radix tree: parent of node (internal i, leaf n-1+k)
