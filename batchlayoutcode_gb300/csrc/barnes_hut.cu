@@ -973,7 +973,10 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs a) {
   if (!block_status_ok(a.st)) return;  // every block sees the same value: no barrier is left waiting
   unsigned int epoch = 0;
   const int gsz = gridDim.x * blockDim.x;
-  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  // slot group k (32 consecutive slots of a level) goes to warp k / gridDim.x
+  // of block k % gridDim.x: a small level spreads over every SM instead of
+  // filling the first blocks
+  const int t0 = (((int)threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x) * 32 + ((int)threadIdx.x & 31);
   SweepVertex first;
   first.t = -1;
   if (a.levels > 0 && a.level_off[0] + t0 < a.level_off[1]) sweep_load(a, a.level_off[0] + t0, first);
