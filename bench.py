@@ -497,6 +497,50 @@ def run_batched(args, w, ws, rank, local):
         dist.destroy_process_group()
 
 
+# Labels the library times with CUDA events around each stage of a
+# Barnes-Hut iteration (direct launches, not the replayed graph).
+BH_STAGES = ["frame_morton", "lsd_passes", "radix_sort", "gather_tree", "chain_kernel", "centroid_kernel",
+             "scan_layout", "traverse_kernel", "sweep_kernel"]
+
+
+def stage_times(a, w, flush, steps, warmup):
+    """Live microseconds per stage of one Barnes-Hut iteration (L2 flushed
+    before every iteration), and the iteration with direct launches and as
+    the replayed graph."""
+    import torch
+    batch, theta = w["batch"], w["theta"]
+    step = 1.0
+    a.set_graph_mode(False)
+    for _ in range(warmup):
+        a.run_resident(4, 1, batch, theta, step, want_energy=False)
+        step *= 0.999
+    out = {"unit": "us", "iterations_per_stage": steps, "stages": {}}
+    for lab in BH_STAGES:
+        a.kernel_time(lab)
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            a.run_resident(4, 1, batch, theta, step, want_energy=False)
+            step *= 0.999
+        torch.cuda.synchronize()
+        ms, cnt = a.kernel_time()
+        out["stages"][lab] = round(ms / max(cnt, 1) * 1000, 1)
+    for mode in (False, True):
+        a.set_graph_mode(mode)
+        ts = []
+        for _ in range(steps + 2):
+            flush.zero_()
+            torch.cuda.synchronize()
+            a.run_resident(4, 1, batch, theta, step, want_energy=False)
+            step *= 0.999
+            ts.append(a.last_run_ms())
+        ts = sorted(ts[2:])
+        out["graph_iteration" if mode else "direct_iteration"] = round(sum(ts) / len(ts) * 1000, 1)
+    out["note"] = ("lsd_passes is part of radix_sort (which adds the runs of equal high halves); "
+                   "the stages of a direct iteration add up to direct_iteration")
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -506,6 +550,8 @@ def main():
     ap.add_argument("--workload", default="rgg1m", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--stages", action="store_true",
+                    help="Barnes-Hut workloads: print the live time of every stage of one iteration and exit")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()
@@ -550,6 +596,9 @@ def main():
     a = B.Algorithms(g.rowptr, g.colids, device=device)
     a.nCoordinates = xy
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
+    if args.stages and w["algo"] == 4:
+        print(json.dumps(stage_times(a, w, flush, args.steps, args.warmup)))
+        return
     algo, batch, theta = w["algo"], w["batch"], w["theta"]
     ips = w.get("iters_per_step", 1)
     decay = DECAY[algo] ** ips
