@@ -463,14 +463,8 @@ int bl_fa_cache_blocking_minibatch(bl_ctx *ctx, int iterations, int threads, int
 }
 
 static int bh_loop(bl_ctx *ctx, int iterations, int batch, double theta, double *energy) {
-  if (batch < 1) return bl_fail(ctx, BL_ERR_ARG, "batch must be >= 1");
   double step = 1.0;
-  for (int it = 0; it < iterations; it++) {
-    const bool last = it == iterations - 1;
-    if (int rc = bl::bh_iteration(ctx, batch, theta, step, last, last ? energy : nullptr)) return rc;
-    step = step * 0.999;
-  }
-  return 0;
+  return bl::bh_run(ctx, iterations, batch, theta, &step, energy);
 }
 
 int bl_barnes_hut_approximation(bl_ctx *ctx, int iterations, int threads, int batch,
@@ -592,8 +586,8 @@ int bl_barnes_hut_iteration(bl_ctx *ctx, int batch, double theta, double step, d
   if (!ctx) return BL_ERR_ARG;
   if (batch < 1) return bl_fail(ctx, BL_ERR_ARG, "batch must be >= 1");
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
-  double energy = 0.0;
-  if (int rc = bl::bh_iteration(ctx, batch, theta, step, true, &energy)) return rc;
+  double energy = 0.0, s = step;
+  if (int rc = bl::bh_run(ctx, 1, batch, theta, &s, &energy)) return rc;
   if (energy_out) *energy_out = energy;
   return BL_OK;
 }
@@ -661,23 +655,8 @@ int bl_run_resident(bl_ctx *ctx, int algo, int iterations, int batch, double the
   } else if (algo == 5) {
     rc = greedy_loop(ctx, iterations, batch, step, &energy);
   } else if (algo == 4) {
-    if (batch < 1) return bl_fail(ctx, BL_ERR_ARG, "batch must be >= 1");
     double s = step;
-    int it = 0;
-    const bool want_energy = energy_out != nullptr;
-    const int replay = want_energy ? iterations - 1 : iterations;
-    if (ctx->graph_mode && replay > 0) {
-      // iterations without energy read-back replay the captured iteration;
-      // if it cannot be captured, they are launched directly
-      const int r = bl::bh_graph_iterations(ctx, batch, theta, &s, replay);
-      if (r < 0) return r;
-      if (r == 0) it = replay;
-    }
-    for (; it < iterations && rc == 0; it++) {
-      const bool last = want_energy && it == iterations - 1;
-      rc = bl::bh_iteration(ctx, batch, theta, s, last, last ? &energy : nullptr);
-      s = s * 0.999;
-    }
+    rc = bl::bh_run(ctx, iterations, batch, theta, &s, energy_out ? &energy : nullptr);
   } else {
     return bl_fail(ctx, BL_ERR_UNSUPPORTED, "bl_run_resident: algo must be 2, 3, 4, 5, 7 or 8");
   }

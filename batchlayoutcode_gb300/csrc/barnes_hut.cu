@@ -1226,7 +1226,9 @@ int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_en
   std::swap(ctx->pos, ctx->s.pos_alt);
   if (want_energy) {
     if (int rc = energy_reduce(ctx, energy_out)) return rc;
-    return bl_check_status(ctx);
+    // without a destination (a captured iteration) the energy stays in
+    // s.energy for the caller to read after the replay
+    return energy_out ? bl_check_status(ctx) : 0;
   }
   return 0;
 }
@@ -1237,32 +1239,38 @@ int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_en
 // alternate between two buffers and STEP changes.  It is captured once per
 // parity of the position buffers and replayed, STEP being set on the sweep's
 // kernel node before each replay.
+// Captured iterations: [variant][parity], variant 1 also writes the forces
+// and |f|^2 and reduces the energy into s.energy; parity p reads the
+// position buffer that is ctx->pos when (ctx->pos == pos0) == (p == 0).
+// Each is captured the first time it is needed.
 struct BhGraph {
   int batch = -1;
   double theta = 0.0;
-  float2 *pos0 = nullptr;  // ctx->pos of the parity-0 graph
-  cudaGraph_t graph[2] = {nullptr, nullptr};
-  cudaGraphExec_t exec[2] = {nullptr, nullptr};
-  cudaGraphNode_t sweep[2] = {nullptr, nullptr};
-  SweepArgs args[2];
-  cudaKernelNodeParams params[2];
-  long long kernels[2] = {0, 0};
+  float2 *pos0 = nullptr;  // ctx->pos of parity 0
+  cudaGraph_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  cudaGraphExec_t exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  cudaGraphNode_t sweep[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  SweepArgs args[2][2];
+  cudaKernelNodeParams params[2][2];
+  long long kernels[2][2] = {{0, 0}, {0, 0}};
 };
 
 void bh_graph_free(BhGraph *g) {
   if (!g) return;
-  for (int p = 0; p < 2; p++) {
-    if (g->exec[p]) cudaGraphExecDestroy(g->exec[p]);
-    if (g->graph[p]) cudaGraphDestroy(g->graph[p]);
-  }
+  for (int v = 0; v < 2; v++)
+    for (int p = 0; p < 2; p++) {
+      if (g->exec[v][p]) cudaGraphExecDestroy(g->exec[v][p]);
+      if (g->graph[v][p]) cudaGraphDestroy(g->graph[v][p]);
+    }
   delete g;
 }
 
 namespace {
 
-// Capture parity p (positions read from ctx->pos, written to s.pos_alt).
-// Returns 0, or 1 when the iteration cannot be captured (nothing has run).
-int bh_graph_capture(bl_ctx *ctx, BhGraph &G, int p, int batch, double theta) {
+// Capture variant v of the iteration that reads ctx->pos (the parity the
+// context is at).  Returns 0, or 1 when the iteration cannot be captured
+// (nothing has run).
+int bh_graph_capture(bl_ctx *ctx, BhGraph &G, int v, int p, int batch, double theta) {
   float2 *save_pos = ctx->pos, *save_alt = ctx->s.pos_alt;
   const std::string save_timed = ctx->timed_kernel;
   const long long save_launches = ctx->launches;
@@ -1272,13 +1280,13 @@ int bh_graph_capture(bl_ctx *ctx, BhGraph &G, int p, int batch, double theta) {
     ctx->timed_kernel = save_timed;
     return 1;
   }
-  const int rc = bh_iteration(ctx, batch, theta, 1.0, false, nullptr);
+  const int rc = bh_iteration(ctx, batch, theta, 1.0, v == 1, nullptr);
   cudaGraph_t graph = nullptr;
   const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
   ctx->pos = save_pos;
   ctx->s.pos_alt = save_alt;
   ctx->timed_kernel = save_timed;
-  G.kernels[p] = ctx->launches - save_launches;
+  G.kernels[v][p] = ctx->launches - save_launches;
   ctx->launches = save_launches;
   if (rc || e != cudaSuccess || !graph) {
     if (graph) cudaGraphDestroy(graph);
@@ -1297,8 +1305,8 @@ int bh_graph_capture(bl_ctx *ctx, BhGraph &G, int p, int batch, double theta) {
     if (cudaGraphKernelNodeGetParams(nd, &kp) != cudaSuccess) continue;
     if (kp.func == (void *)sweep_kernel) {
       sweep = nd;
-      G.params[p] = kp;
-      G.args[p] = *static_cast<SweepArgs *>(kp.kernelParams[0]);
+      G.params[v][p] = kp;
+      G.args[v][p] = *static_cast<SweepArgs *>(kp.kernelParams[0]);
     }
   }
   cudaGraphExec_t exec = nullptr;
@@ -1307,9 +1315,40 @@ int bh_graph_capture(bl_ctx *ctx, BhGraph &G, int p, int batch, double theta) {
     cudaGetLastError();
     return 1;
   }
-  G.graph[p] = graph;
-  G.exec[p] = exec;
-  G.sweep[p] = sweep;
+  G.graph[v][p] = graph;
+  G.exec[v][p] = exec;
+  G.sweep[v][p] = sweep;
+  return 0;
+}
+
+// The context's graphs for (batch, theta), dropped and started afresh when
+// they or the position buffers changed.
+BhGraph *bh_graph_for(bl_ctx *ctx, int batch, double theta) {
+  BhGraph *G = ctx->bh_graph;
+  const bool fresh = !G || G->batch != batch || G->theta != theta ||
+                     (G->pos0 != ctx->pos && G->pos0 != ctx->s.pos_alt);
+  if (fresh) {
+    bh_graph_free(G);
+    G = ctx->bh_graph = new BhGraph();
+    G->batch = batch;
+    G->theta = theta;
+    G->pos0 = ctx->pos;
+  }
+  return G;
+}
+
+// One replay of variant v with STEP `step`; 1 when it cannot be captured.
+int bh_graph_replay(bl_ctx *ctx, BhGraph *G, int v, int batch, double theta, double step) {
+  const int p = (ctx->pos == G->pos0) ? 0 : 1;
+  if (!G->exec[v][p] && bh_graph_capture(ctx, *G, v, p, batch, theta)) return 1;
+  G->args[v][p].step = (float)step;
+  void *kargs[] = {&G->args[v][p]};
+  cudaKernelNodeParams kp = G->params[v][p];
+  kp.kernelParams = kargs;
+  BL_CUDA(ctx, cudaGraphExecKernelNodeSetParams(G->exec[v][p], G->sweep[v][p], &kp));
+  BL_CUDA(ctx, cudaGraphLaunch(G->exec[v][p], ctx->stream));
+  ctx->launches += G->kernels[v][p];
+  std::swap(ctx->pos, ctx->s.pos_alt);
   return 0;
 }
 
@@ -1322,37 +1361,51 @@ int bh_graph_iterations(bl_ctx *ctx, int batch, double theta, double *step, int 
   if (count <= 0) return 0;
   if (int rc = ensure_bh_scratch(ctx)) return rc;
   if (!level_schedule(ctx, batch)) return -2;
-  BhGraph *G = ctx->bh_graph;
-  const bool fresh = !G || G->batch != batch || G->theta != theta ||
-                     (G->pos0 != ctx->pos && G->pos0 != ctx->s.pos_alt);
-  if (fresh) {
-    bh_graph_free(G);
-    G = ctx->bh_graph = new BhGraph();
-    G->batch = batch;
-    G->theta = theta;
-    G->pos0 = ctx->pos;
-    // parity 1 reads the other buffer
-    std::swap(ctx->pos, ctx->s.pos_alt);
-    const int r1 = bh_graph_capture(ctx, *G, 1, batch, theta);
-    std::swap(ctx->pos, ctx->s.pos_alt);
-    const int r0 = r1 ? 1 : bh_graph_capture(ctx, *G, 0, batch, theta);
-    if (r0 || r1) {
-      bh_graph_free(G);
-      ctx->bh_graph = nullptr;
-      return 1;
-    }
-  }
+  BhGraph *G = bh_graph_for(ctx, batch, theta);
   for (int k = 0; k < count; k++) {
-    const int p = (ctx->pos == G->pos0) ? 0 : 1;
-    G->args[p].step = (float)*step;
-    void *kargs[] = {&G->args[p]};
-    cudaKernelNodeParams kp = G->params[p];
-    kp.kernelParams = kargs;
-    BL_CUDA(ctx, cudaGraphExecKernelNodeSetParams(G->exec[p], G->sweep[p], &kp));
-    BL_CUDA(ctx, cudaGraphLaunch(G->exec[p], ctx->stream));
-    ctx->launches += G->kernels[p];
-    std::swap(ctx->pos, ctx->s.pos_alt);
+    const int r = bh_graph_replay(ctx, G, 0, batch, theta, *step);
+    if (r) return k == 0 ? r : -5;  // a parity that cannot be captured after one that could: not expected
     *step *= 0.999;
+  }
+  return 0;
+}
+
+// One iteration with its energy (as bh_iteration with want_energy) by graph
+// replay.  Returns 0, an error code, or 1 when it cannot be captured.
+int bh_graph_energy_iteration(bl_ctx *ctx, int batch, double theta, double step, double *energy_out) {
+  if (int rc = ensure_bh_scratch(ctx)) return rc;
+  if (!level_schedule(ctx, batch)) return -2;
+  BhGraph *G = bh_graph_for(ctx, batch, theta);
+  if (int r = bh_graph_replay(ctx, G, 1, batch, theta, step)) return r;
+  BL_CUDA(ctx, cudaMemcpyAsync(energy_out, ctx->s.energy, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return bl_check_status(ctx);
+}
+
+// `iterations` Barnes-Hut iterations from STEP *step (times 0.999 after
+// each); the last one's energy into *energy when it is not null.  In graph
+// mode the iterations replay captured graphs (the last one the variant that
+// reduces the energy); an iteration that cannot be captured is launched
+// directly.
+int bh_run(bl_ctx *ctx, int iterations, int batch, double theta, double *step, double *energy) {
+  if (batch < 1) return bl_fail(ctx, -1, "batch must be >= 1");  // BL_ERR_ARG
+  int it = 0;
+  const int replay = energy ? iterations - 1 : iterations;
+  if (ctx->graph_mode && replay > 0) {
+    const int r = bh_graph_iterations(ctx, batch, theta, step, replay);
+    if (r < 0) return r;
+    if (r == 0) it = replay;
+  }
+  for (; it < iterations; it++) {
+    const bool last = energy && it == iterations - 1;
+    int r = 1;
+    if (last && ctx->graph_mode) {
+      r = bh_graph_energy_iteration(ctx, batch, theta, *step, energy);
+      if (r < 0) return r;
+    }
+    if (r == 1)
+      if (int rc = bh_iteration(ctx, batch, theta, *step, last, last ? energy : nullptr)) return rc;
+    *step = *step * 0.999;
   }
   return 0;
 }

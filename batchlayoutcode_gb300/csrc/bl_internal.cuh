@@ -249,7 +249,7 @@ struct bl_ctx {
   bl::Scratch s;
   std::deque<bl::LevelSchedule> schedules;  // stable addresses
   long long launches = 0;
-  bool graph_mode = false;
+  bool graph_mode = true;
   // timing of one kernel family for the roofline
   std::string timed_kernel;
   std::vector<cudaEvent_t> ev_pool;
@@ -301,6 +301,8 @@ void batched_free(BatchedState *b);
 void mpnn_free(MpnnState *m);
 void bh_graph_free(BhGraph *g);
 int bh_graph_iterations(bl_ctx *ctx, int batch, double theta, double *step, int count);
+int bh_graph_energy_iteration(bl_ctx *ctx, int batch, double theta, double step, double *energy_out);
+int bh_run(bl_ctx *ctx, int iterations, int batch, double theta, double *step, double *energy);
 int energy_reduce(bl_ctx *ctx, double *out_host);
 int scan_exclusive_int(bl_ctx *ctx, const int *in, int *out, int n);
 }  // namespace bl

@@ -457,9 +457,8 @@ int bl_learned_layout(bl_ctx *ctx, const float *params, const double *scale_mode
   double e = HUGE_VAL, step = step0;
   int it = 0;
   while (it < max_iterations) {
-    if (int rc = bh_iteration(ctx, batch, theta, step, true, &e)) return rc;
+    if (int rc = bh_run(ctx, 1, batch, theta, &step, &e)) return rc;  // STEP times 0.999
     it++;
-    step *= 0.999;
     if (e <= target_energy) break;
   }
   int fell_back = 0;
@@ -467,10 +466,7 @@ int bl_learned_layout(bl_ctx *ctx, const float *params, const double *scale_mode
     // the plain run: greedy DFS start, STEP from 1 (algorithms.cpp:1020-1072)
     if (int rc = bl_init_dfs(ctx)) return rc;
     step = 1.0;
-    for (int k = 0; k < max_iterations; k++) {
-      if (int rc = bh_iteration(ctx, batch, theta, step, k + 1 == max_iterations, &e)) return rc;
-      step *= 0.999;
-    }
+    if (int rc = bh_run(ctx, max_iterations, batch, theta, &step, &e)) return rc;
     fell_back = 1;
   }
   BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

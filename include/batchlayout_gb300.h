@@ -196,12 +196,15 @@ int bl_run_resident(bl_ctx *ctx, int algo, int iterations, int batch, double the
 /* Device time of the last bl_run_resident call: CUDA events recorded on the
  * context's stream before its first and after its last kernel. */
 int bl_last_run_ms(bl_ctx *ctx, double *ms);
-/* Make bl_run_resident with algo 4 replay a captured CUDA graph of one
- * iteration for all iterations but the last (1), or launch every kernel
- * directly (0, the default).  The graph is captured on first use for the
- * given batch and theta and kept until they change; the results are the same
- * bits either way.  If the iteration cannot be captured the kernels are
- * launched directly. */
+/* Barnes-Hut iterations (bl_run_resident with algo 4,
+ * bl_barnes_hut_iteration, bl_barnes_hut_approximation and the Barnes-Hut
+ * part of bl_approx_cache_block_bh) replay captured CUDA graphs of one
+ * iteration (1, the default: the iterations without energy one graph, the
+ * last iteration the graph that also reduces its energy), or launch every
+ * kernel directly (0).  The graphs are captured on first use for the given
+ * batch and theta and kept until they change; the results are the same bits
+ * either way.  If an iteration cannot be captured its kernels are launched
+ * directly. */
 int bl_set_graph_mode(bl_ctx *ctx, int enabled);
 /* CUDA events around the dominant kernel of the last bl_run_resident call:
  * ms[0] = total milliseconds of that kernel, ms[1] = number of launches. */
