@@ -329,11 +329,28 @@ int bl_num_vertices(const bl_ctx *ctx) { return ctx ? ctx->g.n : 0; }
 
 long long bl_kernel_launches(const bl_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
+// Device address of page-locked host memory the device can read and write
+// (a pinned allocation or registered range with a device mapping), else null:
+// the conversion kernels then work on the host buffer directly instead of a
+// staging copy.
+static void *mapped_host(const void *p) {
+  cudaPointerAttributes pa;
+  if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return pa.type == cudaMemoryTypeHost ? pa.devicePointer : nullptr;
+}
+
 int bl_set_coordinates(bl_ctx *ctx, const double *xy, int n) {
   if (!ctx || !xy || n != ctx->g.n) return bl_fail(ctx, BL_ERR_ARG, "bl_set_coordinates: size mismatch");
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
-  BL_CUDA(ctx, cudaMemcpyAsync(ctx->stage, xy, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
-  to_f32_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(ctx->stage, ctx->pos, n);
+  const double2 *src = static_cast<const double2 *>(mapped_host(xy));
+  if (!src) {
+    BL_CUDA(ctx, cudaMemcpyAsync(ctx->stage, xy, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+    src = ctx->stage;
+  }
+  to_f32_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(src, ctx->pos, n);
   ctx->launches++;
   BL_CUDA(ctx, cudaGetLastError());
   BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -343,9 +360,11 @@ int bl_set_coordinates(bl_ctx *ctx, const double *xy, int n) {
 int bl_get_coordinates(bl_ctx *ctx, double *xy, int n) {
   if (!ctx || !xy || n != ctx->g.n) return bl_fail(ctx, BL_ERR_ARG, "bl_get_coordinates: size mismatch");
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
-  to_f64_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(ctx->pos, ctx->stage, n);
+  double2 *dst = static_cast<double2 *>(mapped_host(xy));
+  to_f64_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(ctx->pos, dst ? dst : ctx->stage, n);
   ctx->launches++;
-  BL_CUDA(ctx, cudaMemcpyAsync(xy, ctx->stage, (size_t)n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+  if (!dst)
+    BL_CUDA(ctx, cudaMemcpyAsync(xy, ctx->stage, (size_t)n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
   BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return BL_OK;
 }

@@ -1377,9 +1377,12 @@ int bh_graph_energy_iteration(bl_ctx *ctx, int batch, double theta, double step,
   if (!level_schedule(ctx, batch)) return -2;
   BhGraph *G = bh_graph_for(ctx, batch, theta);
   if (int r = bh_graph_replay(ctx, G, 1, batch, theta, step)) return r;
+  // the energy and the device status in one wait
+  DevStatus st;
   BL_CUDA(ctx, cudaMemcpyAsync(energy_out, ctx->s.energy, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  BL_CUDA(ctx, cudaMemcpyAsync(&st, ctx->s.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, ctx->stream));
   BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  return bl_check_status(ctx);
+  return st.code == 0u ? 0 : bl_check_status(ctx);
 }
 
 // `iterations` Barnes-Hut iterations from STEP *step (times 0.999 after

@@ -404,3 +404,28 @@ def test_graph_mode_replays_the_same_iterations(B):
             out[mode] = (e1, e2, a.nCoordinates)
     assert out[True][0] == out[False][0] and out[True][1] == out[False][1]
     assert np.array_equal(out[True][2], out[False][2])
+
+
+def test_pinned_host_buffers_match_pageable(B):
+    """bl_set_coordinates / bl_get_coordinates on page-locked host memory
+    (converted in place by the device) give the bits of the staged copies
+    made for ordinary host memory."""
+    import torch
+    from batchlayoutcode_gb300 import graphs as G
+    g = G.random_geometric(30_000, 6.0, seed=8)
+    xy = np.asarray(G.init_square(g.n, seed=8), np.float64)
+    pin_in = torch.empty((g.n, 2), dtype=torch.float64, pin_memory=True)
+    pin_out = torch.empty((g.n, 2), dtype=torch.float64, pin_memory=True)
+    pin_in.copy_(torch.from_numpy(xy))
+    with B.Algorithms(g.rowptr, g.colids) as a:
+        a.nCoordinates = xy
+        ref_in = a.nCoordinates  # FP32 round trip through the staged copies
+        a.barnes_hut_iteration(256, 1.2, 1.0)
+        ref_out = a.nCoordinates
+    with B.Algorithms(g.rowptr, g.colids) as a:
+        a.set_coordinates_ptr(pin_in.data_ptr())
+        a.get_coordinates_ptr(pin_out.data_ptr())
+        assert np.array_equal(pin_out.numpy(), ref_in)
+        a.barnes_hut_iteration(256, 1.2, 1.0)
+        a.get_coordinates_ptr(pin_out.data_ptr())
+        assert np.array_equal(pin_out.numpy(), ref_out)
