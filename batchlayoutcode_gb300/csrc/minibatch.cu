@@ -52,6 +52,10 @@ constexpr int kMaxBatch = 4096;
 // the total does not depend on the order of the atomics and stays
 // deterministic.  A partial beyond +-2^34 (forces of ~1e10, coincident
 // vertices) is reported as an error instead of wrapping.
+// Every buffer of accumulators has kAccCopies copies; block s adds into copy
+// s % kAccCopies, so fewer blocks queue on one address at the same time, and
+// the owners add the copies up (integer sums: exact in any order).
+constexpr int kAccCopies = 8;
 constexpr float kFixScale = 268435456.0f;        // 2^28
 constexpr double kFixInv = 1.0 / 268435456.0;    // 2^-28
 constexpr float kFixLimit = 17179869184.0f;      // 2^34
@@ -74,7 +78,7 @@ struct MinibatchArgs {
   float2 *pos;
   double2 *force;
   double *e;
-  long long *acc;         // [2][batch][2] fixed-point force sums (2^-28 units)
+  long long *acc;         // [2][kAccCopies][batch][2] fixed-point force sums (2^-28 units)
   double *energy;         // energy per iteration (device)
   double *energy_parts;   // [grid]
   long long *loops;       // iterations run (device, 1 value)
@@ -330,7 +334,7 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
             o0.x += u0.x; o0.y += u0.y;
             o1.x += u1.x; o1.y += u1.y;
           }
-          long long *A = a.acc + (size_t)buf * a.batch * 2;
+          long long *A = a.acc + ((size_t)buf * kAccCopies + s % kAccCopies) * a.batch * 2;
           if (t0 < cnt) {
             acc_add(&A[2 * t0], o0.x, a.st);
             acc_add(&A[2 * t0 + 1], o0.y, a.st);
@@ -363,13 +367,20 @@ __global__ void __launch_bounds__(kThreads, 1) minibatch_kernel(MinibatchArgs a)
       // ---- owners: read the summed force, update, clear the accumulator -----
       const int olo = max(slo, base), ohi = min(shi, base + cnt);
       if (olo < ohi) {
-        long long *A = a.acc + (size_t)buf * a.batch * 2;
+        long long *A = a.acc + (size_t)buf * kAccCopies * a.batch * 2;
         const float stepf = (float)step;
         for (int i = olo + tid; i < ohi; i += kThreads) {
           const int t = i - base;
-          const longlong2 v = __ldcg(reinterpret_cast<const longlong2 *>(&A[2 * t]));
-          // cleared for the batch after next, which reuses this buffer
-          *reinterpret_cast<longlong2 *>(&A[2 * t]) = make_longlong2(0, 0);
+          longlong2 v = make_longlong2(0, 0);
+#pragma unroll
+          for (int k = 0; k < kAccCopies; k++) {
+            long long *Ak = A + (size_t)k * a.batch * 2;
+            const longlong2 u = __ldcg(reinterpret_cast<const longlong2 *>(&Ak[2 * t]));
+            // cleared for the batch after next, which reuses this buffer
+            *reinterpret_cast<longlong2 *>(&Ak[2 * t]) = make_longlong2(0, 0);
+            v.x += u.x;
+            v.y += u.y;
+          }
           const double dfx = (double)v.x * kFixInv, dfy = (double)v.y * kFixInv;
           const float2 pi = tpos[t];
           const float fx = (float)dfx, fy = (float)dfy;
@@ -443,7 +454,7 @@ __global__ void cursor_table_kernel(const int *__restrict__ rowptr, const int *_
 
 int ensure_minibatch_scratch(bl_ctx *ctx, int batch, int grid) {
   (void)grid;
-  const size_t need = (size_t)2 * batch * 2 * sizeof(long long);
+  const size_t need = (size_t)2 * kAccCopies * batch * 2 * sizeof(long long);
   if (ctx->s.partials_bytes < need) {
     if (ctx->s.partials) cudaFree(ctx->s.partials);
     ctx->s.partials = nullptr;
@@ -515,7 +526,8 @@ int minibatch_run(bl_ctx *ctx, int model, int batch, int iterations, double step
     cursor_grid = grid;
   }
   BL_CUDA(ctx, cudaMemsetAsync(ctx->s.status, 0, sizeof(DevStatus), ctx->stream));
-  BL_CUDA(ctx, cudaMemsetAsync(ctx->s.partials, 0, (size_t)2 * batch * 2 * sizeof(long long), ctx->stream));
+  BL_CUDA(ctx, cudaMemsetAsync(ctx->s.partials, 0, (size_t)2 * kAccCopies * batch * 2 * sizeof(long long),
+                               ctx->stream));
 
   MinibatchArgs a;
   a.n = n;
@@ -588,6 +600,8 @@ constexpr int kNoAllocMaxBatch = 256;
 constexpr int kNoAllocMaxGrid = 160;
 constexpr size_t kNoAllocPartialBytes = (size_t)2 * kNoAllocMaxBatch * kNoAllocMaxGrid * sizeof(float2);
 constexpr size_t kNoAllocBytes = 768 * 1024;
+static_assert((size_t)2 * kAccCopies * kNoAllocMaxBatch * 2 * sizeof(long long) <= kNoAllocPartialBytes,
+              "no-alloc accumulators too small");
 static_assert(kNoAllocPartialBytes + kNoAllocMaxGrid * sizeof(double) + 4 * sizeof(double) +
                       sizeof(DevStatus) <= kNoAllocBytes,
               "no-alloc scratch too small");
@@ -654,7 +668,7 @@ extern "C" int bl_minibatch_iteration_noalloc(int n, const int *d_rowptr, const 
   // the status word (barrier counter, error code) and the force accumulators
   // must start at zero; every other scratch value is written before it is read
   if (cudaMemsetAsync(status, 0, sizeof(DevStatus), st) != cudaSuccess) return BL_ERR_CUDA;
-  if (cudaMemsetAsync(partials, 0, (size_t)2 * batch * 2 * sizeof(long long), st) != cudaSuccess)
+  if (cudaMemsetAsync(partials, 0, (size_t)2 * kAccCopies * batch * 2 * sizeof(long long), st) != cudaSuccess)
     return BL_ERR_CUDA;
   MinibatchArgs a;
   a.n = n;
