@@ -1156,8 +1156,9 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
 int bh_traverse(bl_ctx *ctx, double theta, bool want_stats, int batch) {
   const int n = ctx->g.n;
   Scratch &s = ctx->s;
-  if (n < 2) {
+  if (n < 2) {  // one vertex: no repulsion and no neighbour
     BL_CUDA(ctx, cudaMemsetAsync(s.rep, 0, sizeof(float2) * std::max(n, 1), ctx->stream));
+    if (batch > 0) BL_CUDA(ctx, cudaMemsetAsync(s.f0, 0, sizeof(float4) * std::max(n, 1), ctx->stream));
     return 0;
   }
   TraverseArgs a;
