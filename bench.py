@@ -73,6 +73,19 @@ KERNEL_FOR_ALGO = {4: "traverse_kernel", 2: "minibatch_kernel", 3: "minibatch_ke
 DECAY = {2: 0.999, 4: 0.999, 7: 0.999, 3: 0.99, 8: 0.99, 5: 0.99}
 
 
+def replica_throughput(dist, ws, units_per_step, steps, total_ms, device):
+    """Whole-job throughput of `ws` independent replicas that each ran
+    `steps` steps of `units_per_step` units: the job takes as long as its
+    slowest rank (all-reduce MAX of the timed milliseconds).  Returns
+    (units per second, job milliseconds)."""
+    if dist:
+        import torch
+        t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return ws * units_per_step * steps / (total_ms / 1e3), total_ms
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -414,12 +427,8 @@ def run_batched(args, w, ws, rank, local):
     torch.cuda.synchronize()
     cyc = bl.graph_cycles().astype(np.float64)
     launches = bl.kernel_launches() - launches0
-    total_s = sum(times)
-    if dist:
-        t = torch.tensor([total_s], device=f"cuda:{device}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = ws * nv * iters * args.steps / total_s
+    value, total_ms = replica_throughput(dist, ws, nv * iters, args.steps, 1e3 * sum(times), f"cuda:{device}")
+    total_s = total_ms / 1e3
     clocks = clk.summary()
     sizes = bl.sizes
     small = algo != 4
@@ -644,12 +653,7 @@ def main():
             kstep *= decay
         torch.cuda.synchronize()
     kern_ms, kern_count = a.kernel_time()
-    total_ms = sum(times)
-    if dist:
-        t = torch.tensor([total_ms], device=f"cuda:{device}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = ws * g.n * ips * args.steps / (total_ms / 1e3)
+    value, total_ms = replica_throughput(dist, ws, g.n * ips, args.steps, sum(times), f"cuda:{device}")
     clocks = clk.summary()
 
     # algorithmic bytes of the dominant kernel per launch
