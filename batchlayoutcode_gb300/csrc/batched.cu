@@ -754,7 +754,7 @@ int batched_shape(bl_ctx *ctx, BatchedState &B, int batch) {
 // Per size bucket: time 2 iterations of up to 16 of its minibatch graphs with
 // 1, 2 and 4 source ranges per target and keep the fastest (clock64 cycles
 // per n^2, summed over the sample).
-int batched_autotune(bl_ctx *ctx, BatchedState &B, int batch) {
+int batched_autotune(bl_ctx *ctx, BatchedState &B) {
   for (int bk = 0; bk < 3; bk++) {
     if (B.parts[bk] > 0) continue;
     std::vector<int> sample;
@@ -921,7 +921,7 @@ int bl_batched_run(bl_ctx *ctx, int iterations, int batch, double theta, double 
   a.theta = theta;
   a.theta2 = (float)(theta * theta);
   if (int rc = batched_shape(ctx, *B, batch)) return rc;
-  if (int rc = batched_autotune(ctx, *B, batch)) return rc;
+  if (int rc = batched_autotune(ctx, *B)) return rc;
   if (B->graph_dirty || B->key_iterations != iterations || B->key_batch != batch || B->key_theta != theta ||
       B->key_weight != weight) {
     if (B->exec) cudaGraphExecDestroy(B->exec);
