@@ -213,3 +213,62 @@ def test_grid_generator_sizes():
     assert np.all(np.diff(g.rowptr) > 0)
     xy = G.init_disc(1000, 1)
     assert xy.dtype == np.float32 and np.all((xy.astype(np.float64) ** 2).sum(1) <= 9.0 + 1e-6)
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include <stdlib.h>
+#include "batchlayout_gb300.h"
+
+int main(int argc, char **argv) {
+  long long info[4];
+  double secs = 0.0, *xy;
+  int *rowptr = NULL, *colids = NULL;
+  char err[256];
+  if (argc < 2) return 2;
+  if (bl_read_matrix_market(argv[1], info, &secs, &rowptr, &colids, err, (int)sizeof(err)) != BL_OK) return 3;
+  xy = (double *)malloc(sizeof(double) * 2 * (size_t)info[0]);
+  if (!xy) return 6;
+  if (bl_random_coordinates((int)info[0], xy) != BL_OK) return 4;
+  if (bl_greedy_coordinates((int)info[0], rowptr, colids, xy) != BL_OK) return 5;
+  printf("%lld %lld %d %.17g %.17g\n", info[0], info[2], rowptr[info[0]], xy[0], xy[1]);
+  free(xy);
+  bl_free(rowptr);
+  bl_free(colids);
+  return 0;
+}
+"""
+
+
+def test_c_caller_compiles_links_and_runs(tmp_path, L):
+    """A plain C99 program against include/batchlayout_gb300.h and the shared
+    library: the reader and the host-only greedy start (no GPU involved) give
+    what the Python binding gives."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        pytest.skip("no C compiler")
+    libdir = os.path.join(ROOT, "batchlayoutcode_gb300", "_build")
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        str(src), "-L", libdir, "-lbatchlayout_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    mtx = os.path.join(ROOT, "tests", "golden", "grid12.mtx")
+    r = subprocess.run([str(exe), mtx], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, (r.returncode, r.stderr)
+    n, nnz, rp_last, x0, y0 = r.stdout.split()
+    import batchlayoutcode_gb300 as B
+    rowptr, colids, info = B.read_matrix_market(mtx)
+    assert int(n) == len(rowptr) - 1 and int(rp_last) == len(colids)
+    from batchlayoutcode_gb300 import _lib
+    lib = _lib.load()
+    import ctypes as C
+    import numpy as np
+    xy = np.zeros(2 * (len(rowptr) - 1))
+    assert lib.bl_greedy_coordinates(len(rowptr) - 1, np.ascontiguousarray(rowptr, np.int32).ctypes.data_as(
+        C.POINTER(C.c_int)), np.ascontiguousarray(colids, np.int32).ctypes.data_as(C.POINTER(C.c_int)),
+        xy.ctypes.data_as(C.POINTER(C.c_double))) == 0
+    assert float(x0) == xy[0] and float(y0) == xy[1]
