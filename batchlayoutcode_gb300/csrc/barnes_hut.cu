@@ -495,8 +495,11 @@ __device__ __forceinline__ int kdelta(const u64 *__restrict__ K, int n, int i, i
 // internal node i in [0, n-2]; leaf k encoded as ~k in child links;
 // parent[] holds internal parents of internal nodes (index i) and of leaves
 // (index n-1+k); the root is internal node 0.
+// bnode: the same per internal node packed in 32 bytes for the chain walk,
+// ints {first, last, prefix length, parent, left, right, -, -} (the parent
+// word is written by the parent's thread).
 __global__ void radix_tree_kernel(const u64 *__restrict__ K, int n, int2 *child, int2 *range,
-                                  int *dlt, int *parent) {
+                                  int *dlt, int *parent, int *bnode) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n - 1) return;
   const int d = (kdelta(K, n, i, i + 1) - kdelta(K, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -524,6 +527,15 @@ __global__ void radix_tree_kernel(const u64 *__restrict__ K, int n, int2 *child,
   parent[left >= 0 ? left : (n - 1 + ~left)] = i;
   parent[right >= 0 ? right : (n - 1 + ~right)] = i;
   if (i == 0) parent[0] = -1;
+  int *b = bnode + 8 * (size_t)i;
+  b[0] = first;
+  b[1] = last;
+  b[2] = dnode;
+  b[4] = left;
+  b[5] = right;
+  if (left >= 0) bnode[8 * (size_t)left + 3] = i;
+  if (right >= 0) bnode[8 * (size_t)right + 3] = i;
+  if (i == 0) b[3] = -1;
 }
 
 struct TreeArgs {
@@ -540,6 +552,7 @@ struct TreeArgs {
   int *qpar;     // quad parent of internal node i (index i) and of leaf k (index n-1+k); -1 for the root
   int *qnchild;  // children of a quad node
   int *qarrive;  // children whose centroid is done (zero before the pass)
+  const int4 *bnode;  // packed internal nodes, two int4 each (radix_tree_kernel)
   DevStatus *st;
 };
 
@@ -570,23 +583,46 @@ __global__ void __launch_bounds__(256) chain_kernel(TreeArgs t) {
   int cnt = 0;
   int cur = t.parent[t.n - 1 + k];
   if (k == 0) t.qpar[0] = -1;  // the root
-  // bounded by the tree height: every step moves to a parent
-  while (cur >= 0 && t.range[cur].x == k) {
-    if (!is_sub(t, cur)) {
+  const int4 none = make_int4(-1, -1, -1, -1);
+  int4 ra = none, rb = none;  // cur's packed record
+  if (cur >= 0) {
+    ra = __ldg(&t.bnode[2 * cur]);
+    rb = __ldg(&t.bnode[2 * cur + 1]);
+  }
+  // bounded by the tree height: every step moves to a parent.  The parent's
+  // record and the children's are loaded together, one round trip a step.
+  while (cur >= 0 && ra.x == k) {
+    const int par = ra.w;
+    int4 pa = none, pb = none;
+    if (par >= 0) {
+      pa = __ldg(&t.bnode[2 * par]);
+      pb = __ldg(&t.bnode[2 * par + 1]);
+    }
+    const int p = ra.z;
+    const int sides[2] = {rb.x, rb.y};
+    int4 ca[2] = {none, none}, cb[2] = {none, none};
+#pragma unroll
+    for (int h = 0; h < 2; h++)
+      if (p < 64 && sides[h] >= 0) {
+        ca[h] = __ldg(&t.bnode[2 * sides[h]]);
+        cb[h] = __ldg(&t.bnode[2 * sides[h] + 1]);
+      }
+    // cur is merged into its parent's quad node: the x-bit split of the digit
+    // whose y-bit split is the parent, or any split inside a run below its top
+    const bool sub = cur > 0 && (p >= 64 ? pa.z >= 64 : ((p & 1) && pa.z == p - 1));
+    if (!sub) {
       t.qbelow[cur] = cnt++;
       int kids[4] = {kNoChild, kNoChild, kNoChild, kNoChild};
-      const int p = t.dlt[cur];
       int m = 0;
       if (p < 64) {
-        const int2 ab = t.child[cur];
-        const int sides[2] = {ab.x, ab.y};
 #pragma unroll
         for (int h = 0; h < 2; h++) {
           const int c = sides[h];
-          if (c >= 0 && is_sub(t, c)) {
-            const int2 cc = t.child[c];
-            kids[m++] = cc.x;
-            kids[m++] = cc.y;
+          const int pc = ca[h].z;  // the child's prefix length; its parent is cur
+          const bool csub = c > 0 && (pc >= 64 ? p >= 64 : ((pc & 1) && p == pc - 1));
+          if (c >= 0 && csub) {
+            kids[m++] = cb[h].x;
+            kids[m++] = cb[h].y;
           } else {
             kids[m++] = c;
           }
@@ -594,16 +630,17 @@ __global__ void __launch_bounds__(256) chain_kernel(TreeArgs t) {
         for (int c = 0; c < m; c++) t.qpar[kids[c] >= 0 ? kids[c] : t.n - 1 + ~kids[c]] = cur;
       } else {
         // run of identical keys: every point of the range is a child
-        const int2 rg = t.range[cur];
-        for (int q = rg.x; q <= rg.y; q++) t.qpar[t.n - 1 + q] = cur;
-        m = rg.y - rg.x + 1;
+        for (int q = ra.x; q <= ra.y; q++) t.qpar[t.n - 1 + q] = cur;
+        m = ra.y - ra.x + 1;
       }
       t.qkids[cur] = make_int4(kids[0], kids[1], kids[2], kids[3]);
       t.qnchild[cur] = m;
     } else {
       t.qnchild[cur] = 0;  // merged into its parent: not a quad node
     }
-    cur = (cur == 0) ? -1 : t.parent[cur];
+    cur = (cur == 0) ? -1 : par;
+    ra = pa;
+    rb = pb;
   }
   t.startcnt[k] = cnt;
 }
@@ -1015,7 +1052,7 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   fr(s.bparent); fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.qkids); fr(s.qpar); fr(s.qnchild);
   fr(s.qarrive); fr(s.qcen);
   fr(s.qbelow); fr(s.startcnt); fr(s.startbase); fr(s.nodes); fr(s.nodes_c64);
-  fr(s.nodes_lvl); fr(s.rep); fr(s.f0); fr(s.pos_alt); fr(s.runs);
+  fr(s.nodes_lvl); fr(s.rep); fr(s.f0); fr(s.pos_alt); fr(s.runs); fr(s.bnode);
   const size_t nb = (n + kRsTile - 1) / kRsTile;
   s.hist_entries = 256 * std::max<size_t>(nb, 1) + 256;
   const size_t m = std::max<size_t>(n, 2);
@@ -1028,6 +1065,7 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   BL_CUDA(ctx, cudaMalloc(&s.bparent, 2 * m * sizeof(int)));
   BL_CUDA(ctx, cudaMalloc(&s.bchild, m * sizeof(int2)));
   BL_CUDA(ctx, cudaMalloc(&s.brange, m * sizeof(int2)));
+  BL_CUDA(ctx, cudaMalloc(&s.bnode, 2 * m * sizeof(int4)));
   BL_CUDA(ctx, cudaMalloc(&s.bdelta, m * sizeof(int)));
   BL_CUDA(ctx, cudaMalloc(&s.qkids, m * sizeof(int4)));
   BL_CUDA(ctx, cudaMalloc(&s.qpar, 2 * m * sizeof(int)));
@@ -1107,7 +1145,8 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   bl_time_end(ctx, "radix_sort");
   bl_time_begin(ctx, "gather_tree");
   gather_kernel<<<nblk(n, 256), 256, 0, st>>>(pos, s.perm, n, s.spos);
-  radix_tree_kernel<<<nblk(n - 1, 256), 256, 0, st>>>(s.keys, n, s.bchild, s.brange, s.bdelta, s.bparent);
+  radix_tree_kernel<<<nblk(n - 1, 256), 256, 0, st>>>(s.keys, n, s.bchild, s.brange, s.bdelta, s.bparent,
+                                                       reinterpret_cast<int *>(s.bnode));
   bl_time_end(ctx, "gather_tree");
   BL_CUDA(ctx, cudaMemsetAsync(s.qarrive, 0, (size_t)n * sizeof(int), st));
   BL_CUDA(ctx, cudaMemsetAsync(s.startcnt + n, 0, sizeof(int), st));
@@ -1125,6 +1164,7 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   t.qpar = s.qpar;
   t.qnchild = s.qnchild;
   t.qarrive = s.qarrive;
+  t.bnode = s.bnode;
   t.st = s.status;
   bl_time_begin(ctx, "chain_kernel");
   chain_kernel<<<nblk(n, 256), 256, 0, st>>>(t);

@@ -193,6 +193,7 @@ struct Scratch {
   int *perm = nullptr, *perm_alt = nullptr;
   unsigned int *hist = nullptr;  // radix histograms / offsets
   int fk_grid = 0;               // resident blocks of the frame/key kernel
+  int4 *bnode = nullptr;         // packed binary radix nodes for the chain walk
   int *runs = nullptr;           // runs of equal high key halves: count, (start, length) pairs, overflow
   int runs_cap = 0;
   size_t hist_entries = 0;
