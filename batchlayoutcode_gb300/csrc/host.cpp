@@ -1,5 +1,6 @@
 // host.cpp -- MatrixMarket reader, initialisers and writer (host side).
 #include "host.h"
+#include "fmt_g6.h"
 
 #include <stdlib.h>
 #include <sys/stat.h>
@@ -153,20 +154,25 @@ bool write_coordinates(const std::string &input, const std::string &outputdir,
   FILE *f = std::fopen(path_out.c_str(), "wb");
   if (!f) return false;
   // "x\ty\tid\n" with the default ostream formatting of doubles (6
-  // significant digits, the %g conversion), formatted in parallel slices and
-  // written in order
+  // significant digits, the %g conversion, by fmt_g6), formatted in parallel
+  // slices and written in order
   const size_t n = xy.size() / 2;
   const int T = host_threads(n, 65536);
   std::vector<std::string> parts(T);
   parallel_for(T, [&](int k) {
     const size_t lo = n * k / T, hi = n * (k + 1) / T;
     std::string &out = parts[k];
-    out.reserve((hi - lo) * 32);
-    char line[96];
+    out.resize((hi - lo) * 72);  // a line is at most 2 x 32 + 2 + 21 bytes
+    char *w = &out[0];
     for (size_t i = lo; i < hi; i++) {
-      const int len = std::snprintf(line, sizeof(line), "%g\t%g\t%zu\n", xy[2 * i], xy[2 * i + 1], i + 1);
-      out.append(line, (size_t)len);
+      w += bl::fmt_g6(xy[2 * i], w);
+      *w++ = '\t';
+      w += bl::fmt_g6(xy[2 * i + 1], w);
+      *w++ = '\t';
+      w += bl::fmt_u64(i + 1, w);
+      *w++ = '\n';
     }
+    out.resize((size_t)(w - &out[0]));
   });
   bool ok = true;
   for (auto &part : parts)

@@ -272,3 +272,77 @@ def test_c_caller_compiles_links_and_runs(tmp_path, L):
         C.POINTER(C.c_int)), np.ascontiguousarray(colids, np.int32).ctypes.data_as(C.POINTER(C.c_int)),
         xy.ctypes.data_as(C.POINTER(C.c_double))) == 0
     assert float(x0) == xy[0] and float(y0) == xy[1]
+
+
+FMT_HARNESS = r"""
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <random>
+#include "fmt_g6.h"
+
+static long long bad = 0, total = 0;
+static void check(double v) {
+  char a[64], b[64];
+  const int na = std::snprintf(a, sizeof(a), "%g", v);
+  const int nb = bl::fmt_g6(v, b);
+  total++;
+  if (na != nb || std::memcmp(a, b, na) != 0) {
+    if (bad < 10) std::printf("MISMATCH %.17g printf=%.*s fmt=%.*s\n", v, na, a, nb, b);
+    bad++;
+  }
+}
+
+int main() {
+  std::mt19937_64 g(12345);
+  std::uniform_real_distribution<double> u(0.0, 1.0);
+  for (int i = 0; i < 1000000; i++) {  // magnitudes 1e-40 .. 1e40, both signs
+    const double v = (u(g) + 0.05) * std::pow(10.0, (int)(g() % 81) - 40);
+    check(g() & 1 ? v : -v);
+  }
+  for (int i = 0; i < 1000000; i++) {  // raw bit patterns of finite doubles
+    double v;
+    uint64_t b = g();
+    std::memcpy(&v, &b, 8);
+    if (std::isfinite(v)) check(v);
+  }
+  for (int D = 100000; D < 1000000; D++) {  // exact halves at the sixth digit
+    check(D + 0.5);
+    for (int t = 0; t <= 9; t++) check((double)(D * 10LL + 5) * std::pow(10.0, t));
+  }
+  for (int X = -45; X <= 45; X++) {  // around powers of ten and the style switches
+    const double p = std::pow(10.0, X);
+    double v = p;
+    for (int k = 0; k < 50; k++) v = std::nextafter(v, 0.0);
+    for (int k = 0; k < 100; k++) { check(v); check(-v); v = std::nextafter(v, 1e300); }
+    check(p * 0.9999995); check(p * 0.99999949999); check(p * 0.99999950001); check(p * 1.0000005);
+  }
+  check(0.0); check(-0.0); check(1.0); check(-1.0); check(999999.5); check(9999995.0);
+  check(0.0001); check(0.00001); check(123456.0); check(1234567.0);
+  std::printf("%lld %lld\n", bad, total);
+  return 0;
+}
+"""
+
+
+def test_fmt_g6_matches_printf(tmp_path):
+    """The writer's %g formatter against snprintf on ~11M values: random
+    magnitudes and bit patterns, exact halves at the sixth digit (round half
+    to even), neighbours of every power of ten and of the fixed/exponent
+    switch."""
+    import shutil
+    import subprocess
+    if not shutil.which("g++"):
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "fmt.cpp"
+    src.write_text(FMT_HARNESS)
+    exe = tmp_path / "fmt"
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "batchlayoutcode_gb300", "csrc"),
+                        str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().splitlines()
+    bad, total = map(int, lines[-1].split())
+    assert bad == 0, "\n".join(lines[:10])
+    assert total > 10_000_000
