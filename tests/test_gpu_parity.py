@@ -15,7 +15,7 @@ Tolerances (the layout computes forces in FP32 and keeps FP32 coordinates):
   * final energy after a full run: within 0.5% of the mean of an oracle
     ensemble, or within three standard deviations of it where the reference's
     own chaotic spread is wider (a 5e-9 change of the start moves a 144-vertex
-    layout by 1.7 after 10 iterations; see DESIGN.md).
+    layout by 1.7 after 10 iterations).
 """
 import numpy as np
 import pytest
