@@ -550,6 +550,56 @@ def stage_times(a, w, flush, steps, warmup):
     return out
 
 
+def io_times(reps: int = 3) -> dict:
+    """Host-side input and output of the 1M-vertex workload: the MatrixMarket
+    text of the random geometric graph (lower triangle, pattern symmetric)
+    parsed into the sorted, mirrored CSR (parallel slices), the same through
+    the binary CSR cache (first call parses and writes the cache, later calls
+    read it), and the 1M-line `x y id` output file written with the %g
+    formatting of writeToFile.  Median wall time of `reps` calls each."""
+    import numpy as np
+    from batchlayoutcode_gb300 import _lib, graphs as G
+    g, xy = load_workload("rgg1m")
+    tmp = tempfile.mkdtemp(prefix="blio")
+    mtx = os.path.join(tmp, "rgg1m.mtx")
+    G.write_mtx(g, mtx)
+    mtx_bytes = os.path.getsize(mtx)
+
+    def med(f):
+        ts = []
+        for _ in range(reps):
+            t = time.perf_counter()
+            out = f()
+            ts.append(time.perf_counter() - t)
+        return statistics.median(ts), out
+
+    t_parse, (rp, ci, _) = med(lambda: _lib.read_matrix_market(mtx))
+    assert np.array_equal(rp, g.rowptr) and np.array_equal(ci, g.colids)
+    cache = os.path.join(tmp, "cache")
+    os.makedirs(cache)
+    t = time.perf_counter()
+    _, _, info = _lib.read_matrix_market(mtx, cache)
+    t_miss = time.perf_counter() - t
+    assert not info["cached"]
+    t_hit, (rp2, ci2, info2) = med(lambda: _lib.read_matrix_market(mtx, cache))
+    assert info2["cached"] and np.array_equal(rp2, g.rowptr) and np.array_equal(ci2, g.colids)
+    outd = os.path.join(tmp, "out") + os.sep
+    os.makedirs(outd)
+    xy64 = np.ascontiguousarray(xy, dtype=np.float64)
+    t_write, path = med(lambda: _lib.write_coordinates(mtx, outd, "BHMINB", xy64))
+    out_bytes = os.path.getsize(path)
+    import shutil
+    shutil.rmtree(tmp, ignore_errors=True)
+    ms = lambda x: round(x * 1e3, 2)
+    return {"workload": "rgg1m (%d vertices, %d CSR entries)" % (g.n, g.colids.size),
+            "host_threads": os.cpu_count(), "reps": reps,
+            "parse_mtx_ms": ms(t_parse), "mtx_bytes": mtx_bytes,
+            "parse_mtx_MBps": round(mtx_bytes / t_parse / 1e6, 1),
+            "csr_cache_miss_ms": ms(t_miss), "csr_cache_hit_ms": ms(t_hit),
+            "write_coordinates_ms": ms(t_write), "output_bytes": out_bytes,
+            "write_MBps": round(out_bytes / t_write / 1e6, 1)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -561,7 +611,13 @@ def main():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--stages", action="store_true",
                     help="Barnes-Hut workloads: print the live time of every stage of one iteration and exit")
+    ap.add_argument("--io", action="store_true",
+                    help="host only: time the MatrixMarket reader, the binary CSR cache and the output writer "
+                         "on the 1M-vertex graph, print one JSON line and exit")
     args = ap.parse_args()
+    if args.io:
+        print(json.dumps({"io": io_times()}))
+        return
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()
     w = WORKLOADS[args.workload]

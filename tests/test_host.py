@@ -346,3 +346,19 @@ def test_fmt_g6_matches_printf(tmp_path):
     bad, total = map(int, lines[-1].split())
     assert bad == 0, "\n".join(lines[:10])
     assert total > 10_000_000
+
+
+def test_bench_io_mode(L):
+    """bench.py --io (host only) parses the 1M-vertex graph's MatrixMarket
+    text, checks the CSR against the generator's, goes through the binary
+    cache and writes the 1M-line output file."""
+    import json
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--io"], capture_output=True, text=True,
+                       cwd=ROOT, timeout=600)
+    assert r.returncode == 0, r.stderr
+    io = json.loads(r.stdout.strip().splitlines()[-1])["io"]
+    assert io["mtx_bytes"] > 30_000_000 and io["output_bytes"] > 20_000_000
+    for k in ("parse_mtx_ms", "csr_cache_miss_ms", "csr_cache_hit_ms", "write_coordinates_ms"):
+        assert io[k] > 0
