@@ -68,6 +68,115 @@ def test_reader_errors(L, tmp_path):
         L.read_matrix_market(str(p))
 
 
+MALFORMED = {
+    "empty": "",
+    "banner only": "%%MatrixMarket matrix coordinate pattern symmetric\n",
+    "no entries": "%%MatrixMarket matrix coordinate pattern symmetric\n10 10 3\n",
+    "negative sizes": "%%MatrixMarket matrix coordinate pattern symmetric\n-5 -5 1\n1 2\n",
+    "row past the size": "%%MatrixMarket matrix coordinate pattern symmetric\n4 4 2\n1 2\n9 1\n",
+    "zero index": "%%MatrixMarket matrix coordinate pattern symmetric\n4 4 2\n0 2\n3 1\n",
+    "negative index": "%%MatrixMarket matrix coordinate pattern symmetric\n4 4 2\n-1 2\n3 1\n",
+    "letters": "%%MatrixMarket matrix coordinate pattern symmetric\n4 4 2\nab cd\n3 1\n",
+    "one column": "%%MatrixMarket matrix coordinate pattern symmetric\n4 4 2\n2\n3 1\n",
+    "index overflow": "%%MatrixMarket matrix coordinate pattern symmetric\n4 4 1\n99999999999999999999 1\n",
+    "too few entries": "%%MatrixMarket matrix coordinate pattern symmetric\n4 4 5\n2 1\n3 1\n",
+    "nnz past the file": "%%MatrixMarket matrix coordinate pattern symmetric\n10 10 9000000000000\n1 2\n",
+    "array format": "%%MatrixMarket matrix array real general\n2 2\n1\n2\n3\n4\n",
+    "no banner": "hello\n4 4 1\n2 1\n",
+}
+
+
+@pytest.mark.parametrize("name", sorted(MALFORMED))
+def test_reader_rejects_malformed_files(L, tmp_path, name):
+    p = tmp_path / "m.mtx"
+    p.write_text(MALFORMED[name])
+    with pytest.raises(L.BatchLayoutError):
+        L.read_matrix_market(str(p))
+    with pytest.raises(L.BatchLayoutError):  # and nothing is cached for it
+        L.read_matrix_market(str(p), str(tmp_path))
+
+
+def test_reader_tolerates_line_variants(L, tmp_path):
+    """CRLF line ends, no final newline, comments before and between entries,
+    a value missing on a real line, entries past nnz (ignored)."""
+    p = tmp_path / "v.mtx"
+    for txt in ["%%MatrixMarket matrix coordinate pattern symmetric\r\n4 4 2\r\n2 1\r\n3 1\r\n",
+                "%%MatrixMarket matrix coordinate pattern symmetric\n4 4 2\n2 1\n3 1",
+                "%%MatrixMarket matrix coordinate pattern symmetric\n% a\n%b\n4 4 2\n% c\n2 1\n3 1\n",
+                "%%MatrixMarket matrix coordinate real symmetric\n4 4 2\n2 1 0.5\n3 1\n",
+                "%%MatrixMarket matrix coordinate pattern symmetric\n4 4 2\n2 1\n3 1\n4 1\n"]:
+        p.write_text(txt)
+        rp, ci, info = L.read_matrix_market(str(p))
+        assert rp.tolist() == [0, 2, 3, 4, 4] and ci.tolist() == [1, 2, 0, 0], repr(txt)
+
+
+MUTATE = r"""
+import random, sys
+sys.path.insert(0, sys.argv[1])
+from batchlayoutcode_gb300 import _lib
+base = open(sys.argv[2], "rb").read()
+rng = random.Random(7)
+ok = err = 0
+for k in range(300):
+    b = bytearray(base)
+    op = rng.randrange(3)
+    if op == 0:
+        b = b[: rng.randrange(len(b))]
+    elif op == 1:
+        for _ in range(rng.randrange(1, 20)):
+            b[rng.randrange(len(b))] = rng.choice(b"0123456789 \n-%abc\t.e+")
+    else:
+        i = rng.randrange(len(b))
+        b = b[:i] + bytes(rng.choice(b"0123456789 \n-") for _ in range(rng.randrange(1, 30))) + b[i:]
+    open(sys.argv[3], "wb").write(bytes(b))
+    try:
+        rp, ci, info = _lib.read_matrix_market(sys.argv[3])
+        assert rp[0] == 0 and rp[-1] == len(ci) and (len(ci) == 0 or (ci.min() >= 0 and ci.max() < info["cols"]))
+        ok += 1
+    except _lib.BatchLayoutError:
+        err += 1
+print(ok, err)
+"""
+
+
+def test_reader_survives_mutated_files(L, tmp_path):
+    """300 seeded truncations, byte flips and insertions of a valid file, in a
+    child process: each either parses into a consistent CSR or is rejected
+    with an error; none crashes."""
+    import sys
+    src = tmp_path / "mutate.py"
+    src.write_text(MUTATE)
+    r = subprocess.run([sys.executable, str(src), ROOT, os.path.join(GOLDEN, "grid12.mtx"), str(tmp_path / "x.mtx")],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    ok, err = map(int, r.stdout.split())
+    assert ok + err == 300 and ok > 0 and err > 0
+
+
+def test_create_rejects_invalid_csr(L):
+    """bl_algorithms_create checks the CSR before any device call: every
+    rejection below happens without a GPU and names its reason."""
+    import ctypes as C
+    lib = L.load()
+
+    def create(n, nnz, rowptr, colids):
+        rp = np.ascontiguousarray(rowptr, np.int32)
+        ci = np.ascontiguousarray(colids if len(colids) else [0], np.int32)
+        ctx = lib.bl_algorithms_create(0, n, nnz, rp.ctypes.data_as(C.POINTER(C.c_int)),
+                                       ci.ctypes.data_as(C.POINTER(C.c_int)), b"g.mtx", b"", 2, 1.0, 0.01, b"")
+        assert not ctx
+        return lib.bl_create_error().decode()
+
+    assert "invalid graph arguments" in create(0, 0, [0], [])
+    assert "invalid graph arguments" in create(3, -1, [0, 0, 0, 0], [])
+    assert "exceeds int32" in create(3, 1 << 31, [0, 0, 0, 0], [])
+    assert "start at 0" in create(3, 2, [1, 1, 2, 2], [1, 0])
+    assert "start at 0" in create(3, 2, [0, 1, 2, 3], [1, 0])
+    assert "not monotone" in create(3, 2, [0, 2, 1, 2], [1, 0])
+    assert "column id out of range" in create(3, 2, [0, 1, 2, 2], [1, 3])
+    assert "column id out of range" in create(3, 2, [0, 1, 2, 2], [-1, 0])
+
+
 def _csr_reference(n, rows, cols, symmetric):
     """The reader's CSR built with numpy (mirror + drop self loops when
     symmetric, rows sorted, duplicates kept)."""
