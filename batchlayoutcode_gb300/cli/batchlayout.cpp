@@ -3,9 +3,10 @@
 // output file names and Results.txt row; the layout runs on the GPU through
 // the C ABI.  -threads is accepted and reported but the GPU ignores it.
 //
-// Algorithms on the GPU path: 2 (and 2 with -engt), 3, 4, 6, 8.  Algorithms
-// 0, 1, 5 and 7 of the reference are not on it; they exit with an error
-// message instead of running elsewhere.
+// Algorithms on the GPU path: 2 (and 2 with -engt), 3, 4, 5, 6, 7, 8.
+// Algorithms 0 and 1 of the reference (sequential and naive) are not on it;
+// they exit with an error message instead of running elsewhere.  As in the
+// reference, -algo outside 0..8 (its 9 and 100 included) becomes 2.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -213,7 +214,7 @@ int main(int argc, char *argv[]) {
     algoname = "BCGRDY";
     if (bl_approx_cache_block_bh(ctx, iterations, numberOfThreads, batchsize, out) != BL_OK)
       die(ctx, "approxCacheBlockBH");
-    std::cout << "80%% - 20%% BH - CB" << std::endl;
+    std::cout << "80%% - 20%% BH - CB" << std::endl;  // the doubled % as printed by algorithms.cpp:1209
     std::cout << "BH-CACHE Approximation Energy:" << out[0] << std::endl;
     std::cout << "BH-CACHE Approximation Wall time required:" << out[1] << std::endl;
     write_out(ctx, "BCAPPROX" + B + "PARAOUT" + std::to_string(iterations));
