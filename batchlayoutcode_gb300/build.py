@@ -35,10 +35,13 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def _run(cmd):
+def _run(cmd, log: str | None = None):
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout)
+    if log:
+        with open(log, "w") as f:
+            f.write(r.stdout)
     return r.stdout
 
 
@@ -49,7 +52,10 @@ def _newer(target: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, ptxas_info: bool = False) -> str:
+def build(verbose: bool = False) -> str:
+    """Compile what changed.  Each CUDA unit's ptxas resource report
+    (registers, spills, shared memory per kernel) is kept beside its object
+    as <unit>.ptxas.txt."""
     os.makedirs(OUT, exist_ok=True)
     nv = nvcc()
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
@@ -60,20 +66,17 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         s = os.path.join(CSRC, src)
         o = os.path.join(OUT, src + ".o")
         objs.append(o)
-        if _newer(o, [s] + headers):
-            cmd = [nv, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
-                   "--expt-relaxed-constexpr", "-c", s, "-o", o]
-            if ptxas_info:
-                cmd.insert(1, "-Xptxas=-v")
-            jobs.append(cmd)
+        if _newer(o, [s] + headers) or not os.path.exists(o[:-2] + ".ptxas.txt"):
+            jobs.append(([nv, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas=-v",
+                          "--expt-relaxed-constexpr", "-c", s, "-o", o], o[:-2] + ".ptxas.txt"))
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OUT, src + ".o")
         objs.append(o)
         if _newer(o, [s] + headers):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-c", s, "-o", o])
+            jobs.append((["g++", "-O2", "-std=c++17", "-fPIC", "-c", s, "-o", o], None))
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
-        outs = list(ex.map(_run, jobs))
+        outs = list(ex.map(lambda j: _run(*j), jobs))
     if verbose:
         for o in outs:
             if o.strip():
@@ -88,5 +91,5 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
 
 
 if __name__ == "__main__":
-    build(verbose=True, ptxas_info="--ptxas" in sys.argv)
+    build(verbose=True)
     print(LIB)
