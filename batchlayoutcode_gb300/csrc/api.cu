@@ -227,32 +227,32 @@ int bl_read_matrix_market_cached(const char *path, const char *cache_dir, long l
 
 void bl_free(void *p) { std::free(p); }
 
+// Vertex ids are int, as the reference's INDEXTYPE, and coordinate arrays
+// are indexed by 2 * id in int arithmetic: at most 2^30 - 1 vertices.
+static constexpr int kMaxVertices = (1 << 30) - 1;
+
+// Checks of a caller's CSR (rowptr[n+1], colids[nnz]) before anything reads
+// it by index: null when valid, else the reason.
+static const char *csr_error(int n, long long nnz, const int *rowptr, const int *colids) {
+  if (n < 1 || nnz < 0 || !rowptr || (nnz > 0 && !colids)) return "invalid graph arguments";
+  if (n > kMaxVertices) return "more than 2^30 - 1 vertices";
+  if (nnz > 2147483647LL) return "nnz exceeds int32 (the reference's INDEXTYPE)";
+  if (rowptr[0] != 0 || rowptr[n] != nnz) return "rowptr must start at 0 and end at nnz";
+  for (int i = 0; i < n; i++)
+    if (rowptr[i + 1] < rowptr[i]) return "rowptr not monotone";
+  for (long long k = 0; k < nnz; k++)
+    if (colids[k] < 0 || colids[k] >= n) return "column id out of range";
+  return nullptr;
+}
+
 bl_ctx *bl_algorithms_create(int device, int n, long long nnz, const int *rowptr,
                              const int *colids, const char *input, const char *outputdir,
                              int init, double weight, double threshold, const char *initfile) {
   g_create_error.clear();
-  if (n < 1 || nnz < 0 || !rowptr || (nnz > 0 && !colids)) {
-    g_create_error = "bl_algorithms_create: invalid graph arguments";
+  if (const char *why = csr_error(n, nnz, rowptr, colids)) {
+    g_create_error = std::string("bl_algorithms_create: ") + why;
     return nullptr;
   }
-  if (nnz > 2147483647LL) {
-    g_create_error = "bl_algorithms_create: nnz exceeds int32 (the reference's INDEXTYPE)";
-    return nullptr;
-  }
-  if (rowptr[0] != 0 || rowptr[n] != nnz) {
-    g_create_error = "bl_algorithms_create: rowptr must start at 0 and end at nnz";
-    return nullptr;
-  }
-  for (int i = 0; i < n; i++)
-    if (rowptr[i + 1] < rowptr[i]) {
-      g_create_error = "bl_algorithms_create: rowptr not monotone";
-      return nullptr;
-    }
-  for (long long k = 0; k < nnz; k++)
-    if (colids[k] < 0 || colids[k] >= n) {
-      g_create_error = "bl_algorithms_create: column id out of range";
-      return nullptr;
-    }
   bl_ctx *ctx = new bl_ctx();
   auto bad = [&](cudaError_t e, const char *what) {
     g_create_error = std::string(what) + ": " + cudaGetErrorString(e);
@@ -402,7 +402,7 @@ int bl_file_initialization(bl_ctx *ctx) {
 }
 
 int bl_random_coordinates(int n, double *xy) {
-  if (n < 0 || (n > 0 && !xy)) return BL_ERR_ARG;
+  if (n < 0 || n > kMaxVertices || (n > 0 && !xy)) return BL_ERR_ARG;
   std::vector<double> v;
   blhost::rand_init(n, v);
   std::memcpy(xy, v.data(), v.size() * sizeof(double));
@@ -410,7 +410,7 @@ int bl_random_coordinates(int n, double *xy) {
 }
 
 int bl_greedy_coordinates(int n, const int *rowptr, const int *colids, double *xy) {
-  if (n < 1 || !rowptr || !xy) return BL_ERR_ARG;
+  if (!xy || !rowptr || n < 1 || n > kMaxVertices || csr_error(n, rowptr[n], rowptr, colids)) return BL_ERR_ARG;
   std::vector<int> rp(rowptr, rowptr + n + 1), ci(colids, colids + rowptr[n]);
   std::vector<double> v;
   blhost::init_dfs(n, rp, ci, v);

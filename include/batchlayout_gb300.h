@@ -43,7 +43,9 @@ typedef struct bl_ctx bl_ctx;
 /* Replaces algorithms::algorithms(A_csr, input, outputd, init, weight, th, ifile)
  * (sample/algorithms.cpp:3-15).  Copies the CSR (rowptr[n+1], colids[nnz],
  * zero-based, as built by SetInputMatricesAsCSR, sample/commonutility.h:45-54)
- * to the device.  init: 0 greedy DFS, 1 random, 2 file (`initfile`).
+ * to the device; 1 <= n <= 2^30 - 1, rowptr[0] = 0, rowptr[n] = nnz,
+ * rowptr non-decreasing, 0 <= colids[k] < n (checked before any device call).
+ * init: 0 greedy DFS, 1 random, 2 file (`initfile`).
  * init 3 (an extension): the learned start, `initfile` naming the model file.
  * Returns NULL on failure (bl_create_error() then holds the reason). */
 bl_ctx *bl_algorithms_create(int device, int n, long long nnz, const int *rowptr,
@@ -102,7 +104,8 @@ int bl_file_initialization(bl_ctx *ctx);
 int bl_bfs_init(bl_ctx *ctx);
 
 /* Host-only forms of the same initialisers and of writeToFile: no context or
- * GPU needed (xy holds 2*n doubles). */
+ * GPU needed (xy holds 2*n doubles; the CSR is checked as in
+ * bl_algorithms_create, BL_ERR_ARG when it fails). */
 int bl_random_coordinates(int n, double *xy);
 int bl_greedy_coordinates(int n, const int *rowptr, const int *colids, double *xy);
 int bl_write_coordinates(const char *input, const char *outputdir, const char *tag,

@@ -175,6 +175,29 @@ def test_create_rejects_invalid_csr(L):
     assert "not monotone" in create(3, 2, [0, 2, 1, 2], [1, 0])
     assert "column id out of range" in create(3, 2, [0, 1, 2, 2], [1, 3])
     assert "column id out of range" in create(3, 2, [0, 1, 2, 2], [-1, 0])
+    assert "2^30 - 1 vertices" in create(1 << 30, 0, [0, 0], [])  # rejected before rowptr[n] is read
+
+
+def test_host_initialisers_reject_invalid_csr(L):
+    """The host-only greedy start checks its CSR like the constructor (an
+    out-of-range id would otherwise index its visited flags out of bounds)."""
+    import ctypes as C
+    lib = L.load()
+    xy = np.zeros(8)
+    dp = xy.ctypes.data_as(C.POINTER(C.c_double))
+
+    def greedy(n, rowptr, colids):
+        rp = np.ascontiguousarray(rowptr, np.int32)
+        ci = np.ascontiguousarray(colids if len(colids) else [0], np.int32)
+        return lib.bl_greedy_coordinates(n, rp.ctypes.data_as(C.POINTER(C.c_int)),
+                                         ci.ctypes.data_as(C.POINTER(C.c_int)) if len(colids) else None, dp)
+
+    assert greedy(3, [0, 1, 2, 2], [1, 0]) == 0
+    assert greedy(3, [0, 1, 2, 2], [1, 7]) != 0
+    assert greedy(3, [0, 2, 1, 2], [1, 0]) != 0
+    assert greedy(3, [0, 1, 2, 2], []) != 0   # entries but no colids
+    assert greedy(1 << 30, [0, 0], []) != 0
+    assert lib.bl_random_coordinates(1 << 30, dp) != 0
 
 
 def _csr_reference(n, rows, cols, symmetric):
