@@ -820,6 +820,7 @@ int bl_batched_prepare(bl_ctx *ctx, int num_graphs, const int *vertex_offset, co
     return bl_fail(ctx, BL_ERR_ARG, "bl_batched_prepare: null argument or no graphs");
   if (edge_offset[num_graphs] > 0 && !colids) return bl_fail(ctx, BL_ERR_ARG, "bl_batched_prepare: null colids");
   if (vertex_offset[0] != 0) return bl_fail(ctx, BL_ERR_ARG, "vertex_offset[0] must be 0");
+  if (edge_offset[0] != 0) return bl_fail(ctx, BL_ERR_ARG, "edge_offset[0] must be 0");
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   batched_free(ctx->batched);
   ctx->batched = nullptr;

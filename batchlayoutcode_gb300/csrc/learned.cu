@@ -242,6 +242,12 @@ int bl_learned_train(bl_ctx *ctx, int num_graphs, const int *vertex_offset, cons
       epochs < 0 || !(lr > 0))
     return BL_ERR_ARG;
   if (vertex_offset[0] != 0) return bl_fail(ctx, BL_ERR_ARG, "vertex_offset[0] must be 0");
+  if (edge_offset[0] != 0 || edge_offset[num_graphs] < 0 || edge_offset[num_graphs] > 2147483647LL)
+    return bl_fail(ctx, BL_ERR_ARG, "edge_offset must start at 0 and end within int32");
+  if (edge_offset[num_graphs] > 0 && !colids) return bl_fail(ctx, BL_ERR_ARG, "null colids");
+  for (int g = 0; g < num_graphs; g++)  // before the offsets size anything
+    if ((long long)vertex_offset[g + 1] - vertex_offset[g] < 2)
+      return bl_fail(ctx, BL_ERR_ARG, "graph " + std::to_string(g) + " has fewer than two vertices");
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   const int N = vertex_offset[num_graphs];
   std::vector<int> grp(N + 1), gci;
