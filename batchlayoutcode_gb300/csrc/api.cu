@@ -7,7 +7,9 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <exception>
 #include <limits>
+#include <new>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -22,6 +24,44 @@ static thread_local std::string g_create_error;
 int bl_fail(bl_ctx *ctx, int code, const std::string &msg) {
   if (ctx) ctx->err = msg;
   return code;
+}
+
+// Host code (allocations, worker threads, strings) may throw; no exception
+// crosses the C ABI.  Each entry point's handler calls one of these: the
+// exception in flight becomes BL_ERR_HOST, its message on the context (or,
+// for a constructor, in bl_create_error()).
+static void describe_exception(char *buf, size_t cap) {
+  try {
+    throw;
+  } catch (const std::bad_alloc &) {
+    std::snprintf(buf, cap, "host exception: memory allocation failed");
+  } catch (const std::exception &e) {
+    std::snprintf(buf, cap, "host exception: %s", e.what());
+  } catch (...) {
+    std::snprintf(buf, cap, "host exception");
+  }
+}
+
+int bl_host_exception(bl_ctx *ctx, char *msg, int msgcap) {
+  char buf[256];
+  describe_exception(buf, sizeof(buf));
+  if (msg && msgcap > 0) std::snprintf(msg, (size_t)msgcap, "%s", buf);
+  if (ctx) {
+    try {
+      ctx->err = buf;
+    } catch (...) {
+    }
+  }
+  return BL_ERR_HOST;
+}
+
+void bl_create_exception() {
+  char buf[256];
+  describe_exception(buf, sizeof(buf));
+  try {
+    g_create_error = buf;
+  } catch (...) {
+  }
 }
 
 int bl_cuda_fail(bl_ctx *ctx, cudaError_t e, const char *what) {
@@ -196,7 +236,7 @@ static int export_csr(const blhost::MatrixInfo &mi, const std::vector<int> &rp, 
 }
 
 int bl_read_matrix_market(const char *path, long long *info, double *seconds, int **rowptr,
-                          int **colids, char *err, int errcap) {
+                          int **colids, char *err, int errcap) try {
   if (!path || !info || !rowptr || !colids) return BL_ERR_ARG;
   blhost::MatrixInfo mi;
   std::vector<int> rp, ci;
@@ -206,10 +246,12 @@ int bl_read_matrix_market(const char *path, long long *info, double *seconds, in
     return BL_ERR_IO;
   }
   return export_csr(mi, rp, ci, info, seconds, rowptr, colids);
+} catch (...) {
+  return bl_host_exception(nullptr, err, errcap);
 }
 
 int bl_read_matrix_market_cached(const char *path, const char *cache_dir, long long *info, double *seconds,
-                                 int **rowptr, int **colids, char *err, int errcap) {
+                                 int **rowptr, int **colids, char *err, int errcap) try {
   if (!path || !info || !rowptr || !colids) return BL_ERR_ARG;
   blhost::MatrixInfo mi;
   std::vector<int> rp, ci;
@@ -223,6 +265,8 @@ int bl_read_matrix_market_cached(const char *path, const char *cache_dir, long l
   }
   info[4] = cached ? 1 : 0;
   return export_csr(mi, rp, ci, info, seconds, rowptr, colids);
+} catch (...) {
+  return bl_host_exception(nullptr, err, errcap);
 }
 
 void bl_free(void *p) { std::free(p); }
@@ -247,7 +291,7 @@ static const char *csr_error(int n, long long nnz, const int *rowptr, const int 
 
 bl_ctx *bl_algorithms_create(int device, int n, long long nnz, const int *rowptr,
                              const int *colids, const char *input, const char *outputdir,
-                             int init, double weight, double threshold, const char *initfile) {
+                             int init, double weight, double threshold, const char *initfile) try {
   g_create_error.clear();
   if (const char *why = csr_error(n, nnz, rowptr, colids)) {
     g_create_error = std::string("bl_algorithms_create: ") + why;
@@ -313,14 +357,18 @@ bl_ctx *bl_algorithms_create(int device, int n, long long nnz, const int *rowptr
   cudaMemset(ctx->s.status, 0, sizeof(DevStatus));
   if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bad(e, "cudaDeviceSynchronize");
   return ctx;
+} catch (...) {
+  bl_create_exception();
+  return nullptr;
 }
 
-void bl_destroy(bl_ctx *ctx) {
+void bl_destroy(bl_ctx *ctx) try {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   free_ctx(ctx);
   delete ctx;
+} catch (...) {
 }
 
 const char *bl_last_error(const bl_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
@@ -342,7 +390,7 @@ static void *mapped_host(const void *p) {
   return pa.type == cudaMemoryTypeHost ? pa.devicePointer : nullptr;
 }
 
-int bl_set_coordinates(bl_ctx *ctx, const double *xy, int n) {
+int bl_set_coordinates(bl_ctx *ctx, const double *xy, int n) try {
   if (!ctx || !xy || n != ctx->g.n) return bl_fail(ctx, BL_ERR_ARG, "bl_set_coordinates: size mismatch");
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   const double2 *src = static_cast<const double2 *>(mapped_host(xy));
@@ -355,9 +403,11 @@ int bl_set_coordinates(bl_ctx *ctx, const double *xy, int n) {
   BL_CUDA(ctx, cudaGetLastError());
   BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_get_coordinates(bl_ctx *ctx, double *xy, int n) {
+int bl_get_coordinates(bl_ctx *ctx, double *xy, int n) try {
   if (!ctx || !xy || n != ctx->g.n) return bl_fail(ctx, BL_ERR_ARG, "bl_get_coordinates: size mismatch");
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   double2 *dst = static_cast<double2 *>(mapped_host(xy));
@@ -367,65 +417,81 @@ int bl_get_coordinates(bl_ctx *ctx, double *xy, int n) {
     BL_CUDA(ctx, cudaMemcpyAsync(xy, ctx->stage, (size_t)n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
   BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_get_forces(bl_ctx *ctx, double *fxy, int n) {
+int bl_get_forces(bl_ctx *ctx, double *fxy, int n) try {
   if (!ctx || !fxy || n != ctx->g.n) return bl_fail(ctx, BL_ERR_ARG, "bl_get_forces: size mismatch");
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   BL_CUDA(ctx, cudaMemcpyAsync(fxy, ctx->force, (size_t)n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
   BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 // ---- initialisers ----------------------------------------------------------
 
-int bl_rand_init(bl_ctx *ctx) {
+int bl_rand_init(bl_ctx *ctx) try {
   if (!ctx) return BL_ERR_ARG;
   std::vector<double> xy;
   blhost::rand_init(ctx->g.n, xy);
   return bl_set_coordinates(ctx, xy.data(), ctx->g.n);
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_init_dfs(bl_ctx *ctx) {
+int bl_init_dfs(bl_ctx *ctx) try {
   if (!ctx) return BL_ERR_ARG;
   std::vector<double> xy;
   blhost::init_dfs(ctx->g.n, ctx->h_rowptr, ctx->h_colids, xy);
   return bl_set_coordinates(ctx, xy.data(), ctx->g.n);
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_file_initialization(bl_ctx *ctx) {
+int bl_file_initialization(bl_ctx *ctx) try {
   if (!ctx) return BL_ERR_ARG;
   std::vector<double> xy(2 * (size_t)ctx->g.n, 0.0);
   std::string msg;
   if (!blhost::file_init(ctx->initfile, ctx->g.n, xy, msg)) return bl_fail(ctx, BL_ERR_IO, msg);
   return bl_set_coordinates(ctx, xy.data(), ctx->g.n);
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_random_coordinates(int n, double *xy) {
+int bl_random_coordinates(int n, double *xy) try {
   if (n < 0 || n > kMaxVertices || (n > 0 && !xy)) return BL_ERR_ARG;
   std::vector<double> v;
   blhost::rand_init(n, v);
   std::memcpy(xy, v.data(), v.size() * sizeof(double));
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(nullptr);
 }
 
-int bl_greedy_coordinates(int n, const int *rowptr, const int *colids, double *xy) {
+int bl_greedy_coordinates(int n, const int *rowptr, const int *colids, double *xy) try {
   if (!xy || !rowptr || n < 1 || n > kMaxVertices || csr_error(n, rowptr[n], rowptr, colids)) return BL_ERR_ARG;
   std::vector<int> rp(rowptr, rowptr + n + 1), ci(colids, colids + rowptr[n]);
   std::vector<double> v;
   blhost::init_dfs(n, rp, ci, v);
   std::memcpy(xy, v.data(), v.size() * sizeof(double));
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(nullptr);
 }
 
 int bl_write_coordinates(const char *input, const char *outputdir, const char *tag, const double *xy,
-                         int n, char *path_out, int path_cap) {
+                         int n, char *path_out, int path_cap) try {
   if (!input || !outputdir || !tag || (n > 0 && !xy)) return BL_ERR_ARG;
   std::vector<double> v(xy, xy + 2 * (size_t)n);
   std::string path;
   const bool ok = blhost::write_coordinates(input, outputdir, tag, v, path);
   if (path_out && path_cap > 0) std::snprintf(path_out, (size_t)path_cap, "%s", path.c_str());
   return ok ? BL_OK : BL_ERR_IO;
+} catch (...) {
+  return bl_host_exception(nullptr);
 }
 
 // ---- layout methods ----------------------------------------------------------
@@ -456,29 +522,37 @@ static int minibatch_method(bl_ctx *ctx, int model, double decay, int iterations
 }
 
 int bl_cache_blocking_minibatch(bl_ctx *ctx, int iterations, int threads, int batch, int flag,
-                                double *out) {
+                                double *out) try {
   (void)threads;
   return minibatch_method(ctx, bl::MODEL_FR, 0.999, iterations, batch, flag, false, out, 0.0);
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 int bl_cache_blocking_minibatch_converged(bl_ctx *ctx, int iterations, int threads, int batch,
-                                          int flag, double *out) {
+                                          int flag, double *out) try {
   (void)threads;
   return minibatch_method(ctx, bl::MODEL_FR, 0.999, iterations, batch, flag, true, out, 0.0);
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 int bl_linlog_cache_blocking_minibatch(bl_ctx *ctx, int iterations, int threads, int batch,
-                                       double *out) {
+                                       double *out) try {
   (void)threads;
   return minibatch_method(ctx, bl::MODEL_LINLOG, 0.99, iterations, batch, 0, false, out,
                           std::numeric_limits<double>::max());
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 int bl_fa_cache_blocking_minibatch(bl_ctx *ctx, int iterations, int threads, int batch,
-                                   double *out) {
+                                   double *out) try {
   (void)threads;
   return minibatch_method(ctx, bl::MODEL_FA, 0.99, iterations, batch, 0, false, out,
                           std::numeric_limits<double>::max());
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 static int bh_loop(bl_ctx *ctx, int iterations, int batch, double theta, double *energy) {
@@ -487,7 +561,7 @@ static int bh_loop(bl_ctx *ctx, int iterations, int batch, double theta, double 
 }
 
 int bl_barnes_hut_approximation(bl_ctx *ctx, int iterations, int threads, int batch,
-                                double theta, int flag, double *out) {
+                                double theta, int flag, double *out) try {
   (void)threads;
   if (!ctx || !out) return BL_ERR_ARG;
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -500,9 +574,11 @@ int bl_barnes_hut_approximation(bl_ctx *ctx, int iterations, int threads, int ba
   out[0] = energy;
   out[1] = wall() - t0;
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_approx_cache_block_bh(bl_ctx *ctx, int iterations, int threads, int batch, double *out) {
+int bl_approx_cache_block_bh(bl_ctx *ctx, int iterations, int threads, int batch, double *out) try {
   (void)threads;
   if (!ctx || !out) return BL_ERR_ARG;
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -522,6 +598,8 @@ int bl_approx_cache_block_bh(bl_ctx *ctx, int iterations, int threads, int batch
   out[0] = energy;
   out[1] = wall() - t0;
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 // Algo 5 from STEP `step`: iterations 0..(int)(0.8*iterations) are the walk
@@ -542,7 +620,7 @@ static int greedy_loop(bl_ctx *ctx, int iterations, int batch, double step, doub
   return 0;
 }
 
-int bl_approx_force_directed(bl_ctx *ctx, int iterations, int threads, int batch, double *out) {
+int bl_approx_force_directed(bl_ctx *ctx, int iterations, int threads, int batch, double *out) try {
   (void)threads;
   if (!ctx || !out) return BL_ERR_ARG;
   if (batch < 1) return bl_fail(ctx, BL_ERR_ARG, "batch must be >= 1");
@@ -555,16 +633,20 @@ int bl_approx_force_directed(bl_ctx *ctx, int iterations, int threads, int batch
   out[0] = energy;
   out[1] = wall() - t0;
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 int bl_cache_blocking_minibatch_sd(bl_ctx *ctx, int iterations, int threads, int batch, int flag,
-                                   double *out) {
+                                   double *out) try {
   (void)threads;
   return minibatch_method(ctx, bl::MODEL_SD, 0.999, iterations, batch, flag, false, out,
                           std::numeric_limits<double>::max());
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_write_to_file(bl_ctx *ctx, const char *tag, char *path_out, int path_cap) {
+int bl_write_to_file(bl_ctx *ctx, const char *tag, char *path_out, int path_cap) try {
   if (!ctx || !tag) return BL_ERR_ARG;
   std::vector<double> xy(2 * (size_t)ctx->g.n);
   if (int rc = bl_get_coordinates(ctx, xy.data(), ctx->g.n)) return rc;
@@ -576,11 +658,13 @@ int bl_write_to_file(bl_ctx *ctx, const char *tag, char *path_out, int path_cap)
     std::snprintf(path_out, (size_t)path_cap, "%s", path.c_str());
   }
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 // ---- building blocks -----------------------------------------------------------
 
-int bl_minibatch_iteration(bl_ctx *ctx, int model, int batch, double step, double *energy_out) {
+int bl_minibatch_iteration(bl_ctx *ctx, int model, int batch, double step, double *energy_out) try {
   if (!ctx) return BL_ERR_ARG;
   if (model != 2 && model != 3 && model != 8 && model != 7 && model != 5)
     return bl_fail(ctx, BL_ERR_ARG, "model must be 2, 3, 5, 7 or 8");
@@ -590,18 +674,22 @@ int bl_minibatch_iteration(bl_ctx *ctx, int model, int batch, double step, doubl
   if (int rc = bl::minibatch_run(ctx, model, batch, 1, step, 1.0, false, 0.0, 0, &energy, &loops)) return rc;
   if (energy_out) *energy_out = energy;
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_greedy_iteration(bl_ctx *ctx, int batch, double step, double *energy_out) {
+int bl_greedy_iteration(bl_ctx *ctx, int batch, double step, double *energy_out) try {
   if (!ctx) return BL_ERR_ARG;
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   double energy = 0.0;
   if (int rc = bl::greedy_walk_run(ctx, batch, 1, step, 1.0, true, &energy)) return rc;
   if (energy_out) *energy_out = energy;
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_barnes_hut_iteration(bl_ctx *ctx, int batch, double theta, double step, double *energy_out) {
+int bl_barnes_hut_iteration(bl_ctx *ctx, int batch, double theta, double step, double *energy_out) try {
   if (!ctx) return BL_ERR_ARG;
   if (batch < 1) return bl_fail(ctx, BL_ERR_ARG, "batch must be >= 1");
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -609,9 +697,11 @@ int bl_barnes_hut_iteration(bl_ctx *ctx, int batch, double theta, double step, d
   if (int rc = bl::bh_run(ctx, 1, batch, theta, &s, &energy)) return rc;
   if (energy_out) *energy_out = energy;
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_morton_order(bl_ctx *ctx, double *frame, unsigned long long *keys, int *perm) {
+int bl_morton_order(bl_ctx *ctx, double *frame, unsigned long long *keys, int *perm) try {
   if (!ctx || !frame || !keys || !perm) return BL_ERR_ARG;
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   const int n = ctx->g.n;
@@ -623,16 +713,20 @@ int bl_morton_order(bl_ctx *ctx, double *frame, unsigned long long *keys, int *p
   BL_CUDA(ctx, cudaMemcpyAsync(perm, ctx->s.perm, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
   BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return bl_check_status(ctx);
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_quadtree(bl_ctx *ctx, int cap, int *lo, int *hi, int *depth, int *nchild, double *centroid) {
+int bl_quadtree(bl_ctx *ctx, int cap, int *lo, int *hi, int *depth, int *nchild, double *centroid) try {
   if (!ctx || cap < 0 || !lo || !hi || !depth || !nchild || !centroid) return BL_ERR_ARG;
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   if (ctx->g.n < 2) return bl_fail(ctx, BL_ERR_ARG, "need at least two vertices");
   return bl::bh_canonical_tree(ctx, cap, lo, hi, depth, nchild, centroid);
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_bh_repulsion(bl_ctx *ctx, double theta, double *out, long long *stats) {
+int bl_bh_repulsion(bl_ctx *ctx, double theta, double *out, long long *stats) try {
   if (!ctx || !out) return BL_ERR_ARG;
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   const int n = ctx->g.n;
@@ -654,10 +748,12 @@ int bl_bh_repulsion(bl_ctx *ctx, double theta, double *out, long long *stats) {
     stats[1] = (long long)st[1];
   }
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 int bl_run_resident(bl_ctx *ctx, int algo, int iterations, int batch, double theta, double step,
-                    double *energy_out) {
+                    double *energy_out) try {
   if (!ctx) return BL_ERR_ARG;
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   if (!ctx->run_ev[0]) {
@@ -689,21 +785,27 @@ int bl_run_resident(bl_ctx *ctx, int algo, int iterations, int batch, double the
   if (energy_out) *energy_out = energy;
   if (algo == 4 && !energy_out) return bl_check_status(ctx);
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_last_run_ms(bl_ctx *ctx, double *ms) {
+int bl_last_run_ms(bl_ctx *ctx, double *ms) try {
   if (!ctx || !ms) return BL_ERR_ARG;
   *ms = ctx->last_run_ms;
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_set_graph_mode(bl_ctx *ctx, int enabled) {
+int bl_set_graph_mode(bl_ctx *ctx, int enabled) try {
   if (!ctx) return BL_ERR_ARG;
   ctx->graph_mode = enabled != 0;
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_last_kernel_time(bl_ctx *ctx, const char *kernel, double *ms) {
+int bl_last_kernel_time(bl_ctx *ctx, const char *kernel, double *ms) try {
   if (!ctx || !ms) return BL_ERR_ARG;
   if (kernel && ctx->timed_kernel != kernel) {
     // start timing this kernel family from now on
@@ -721,6 +823,8 @@ int bl_last_kernel_time(bl_ctx *ctx, const char *kernel, double *ms) {
   ctx->timed_ms = 0.0;
   ctx->timed_count = 0;
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 }  // extern "C"

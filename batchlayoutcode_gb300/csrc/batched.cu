@@ -798,7 +798,7 @@ int batched_autotune(bl_ctx *ctx, BatchedState &B) {
 // ---- C ABI ---------------------------------------------------------------------
 extern "C" {
 
-bl_ctx *bl_batch_create(int device) {
+bl_ctx *bl_batch_create(int device) try {
   bl_ctx *ctx = new bl_ctx();
   ctx->device = device;
   if (cudaSetDevice(device) != cudaSuccess ||
@@ -810,10 +810,13 @@ bl_ctx *bl_batch_create(int device) {
     return nullptr;
   }
   return ctx;
+} catch (...) {
+  bl_create_exception();
+  return nullptr;
 }
 
 int bl_batched_prepare(bl_ctx *ctx, int num_graphs, const int *vertex_offset, const long long *edge_offset,
-                       const int *rowptr, const int *colids, const int *algo, const double *xy) {
+                       const int *rowptr, const int *colids, const int *algo, const double *xy) try {
   using namespace bl;
   if (!ctx) return BL_ERR_ARG;
   if (num_graphs < 1 || !vertex_offset || !edge_offset || !rowptr || !algo || !xy)
@@ -906,9 +909,11 @@ int bl_batched_prepare(bl_ctx *ctx, int num_graphs, const int *vertex_offset, co
   a.st = ctx->s.status;
   BL_CUDA(ctx, cudaStreamSynchronize(st));
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_batched_run(bl_ctx *ctx, int iterations, int batch, double theta, double weight, double *seconds_out) {
+int bl_batched_run(bl_ctx *ctx, int iterations, int batch, double theta, double weight, double *seconds_out) try {
   using namespace bl;
   if (!ctx) return BL_ERR_ARG;
   BatchedState *B = ctx->batched;
@@ -962,9 +967,11 @@ int bl_batched_run(bl_ctx *ctx, int iterations, int batch, double theta, double 
   ctx->last_run_ms = ms;
   if (seconds_out) *seconds_out = ms * 1e-3;
   return bl_check_status(ctx);
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_batched_result(bl_ctx *ctx, double *xy, double *energy) {
+int bl_batched_result(bl_ctx *ctx, double *xy, double *energy) try {
   using namespace bl;
   if (!ctx) return BL_ERR_ARG;
   BatchedState *B = ctx->batched;
@@ -978,17 +985,21 @@ int bl_batched_result(bl_ctx *ctx, double *xy, double *energy) {
                                  ctx->stream));
   BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 int bl_batched_layout(bl_ctx *ctx, int num_graphs, const int *vertex_offset, const long long *edge_offset,
                       const int *rowptr, const int *colids, const int *algo, double *xy, int iterations, int batch,
-                      double theta, double weight, double *energy_out, double *seconds_out) {
+                      double theta, double weight, double *energy_out, double *seconds_out) try {
   if (int rc = bl_batched_prepare(ctx, num_graphs, vertex_offset, edge_offset, rowptr, colids, algo, xy)) return rc;
   if (int rc = bl_batched_run(ctx, iterations, batch, theta, weight, seconds_out)) return rc;
   return bl_batched_result(ctx, xy, energy_out);
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_batched_graph_cycles(bl_ctx *ctx, unsigned long long *cycles) {
+int bl_batched_graph_cycles(bl_ctx *ctx, unsigned long long *cycles) try {
   if (!ctx || !cycles) return BL_ERR_ARG;
   if (!ctx->batched) return bl_fail(ctx, BL_ERR_STATE, "bl_batched_graph_cycles before bl_batched_prepare");
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -996,9 +1007,11 @@ int bl_batched_graph_cycles(bl_ctx *ctx, unsigned long long *cycles) {
                                cudaMemcpyDeviceToHost, ctx->stream));
   BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_batched_set_parts(bl_ctx *ctx, const int *parts3) {
+int bl_batched_set_parts(bl_ctx *ctx, const int *parts3) try {
   if (!ctx || !parts3) return BL_ERR_ARG;
   if (!ctx->batched) return bl_fail(ctx, BL_ERR_STATE, "bl_batched_set_parts before bl_batched_prepare");
   for (int k = 0; k < 3; k++)
@@ -1006,12 +1019,16 @@ int bl_batched_set_parts(bl_ctx *ctx, const int *parts3) {
       return bl_fail(ctx, BL_ERR_ARG, "parts must be 0 (autotune), 1, 2 or 4");
   for (int k = 0; k < 3; k++) ctx->batched->parts[k] = parts3[k];
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_batched_parts(const bl_ctx *ctx, int *parts3) {
+int bl_batched_parts(const bl_ctx *ctx, int *parts3) try {
   if (!ctx || !parts3) return BL_ERR_ARG;
   for (int k = 0; k < 3; k++) parts3[k] = ctx->batched ? ctx->batched->parts[k] : 0;
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(nullptr);
 }
 
 }  // extern "C"

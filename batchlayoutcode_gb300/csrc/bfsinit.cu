@@ -324,8 +324,10 @@ int bfs_init(bl_ctx *ctx) {
 
 }  // namespace bl
 
-extern "C" int bl_bfs_init(bl_ctx *ctx) {
+extern "C" int bl_bfs_init(bl_ctx *ctx) try {
   if (!ctx) return BL_ERR_ARG;
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   return bl::bfs_init(ctx);
+} catch (...) {
+  return bl_host_exception(ctx);
 }

@@ -267,6 +267,9 @@ struct bl_ctx {
 // ---- helpers implemented in api.cu ---------------------------------------
 int bl_fail(bl_ctx *ctx, int code, const std::string &msg);
 int bl_cuda_fail(bl_ctx *ctx, cudaError_t e, const char *what);
+// inside a catch: BL_ERR_HOST, the message on ctx and in msg (msgcap bytes)
+int bl_host_exception(bl_ctx *ctx, char *msg = nullptr, int msgcap = 0);
+void bl_create_exception();          // inside a catch: message for bl_create_error()
 int bl_check_status(bl_ctx *ctx);
 void bl_time_begin(bl_ctx *ctx, const char *kernel);
 void bl_time_end(bl_ctx *ctx, const char *kernel);

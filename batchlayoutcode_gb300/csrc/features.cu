@@ -471,7 +471,7 @@ int compute_features(bl_ctx *ctx, int num_graphs, const int *voff, int n, const 
 extern "C" {
 
 int bl_learned_features(bl_ctx *ctx, int n, const int *rowptr, const int *colids, int seed, const int *pivots,
-                        float *features, unsigned short *dist, int *pivots_out) {
+                        float *features, unsigned short *dist, int *pivots_out) try {
   using namespace bl;
   if (!ctx || n < 1 || !rowptr || !features) return BL_ERR_ARG;
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -518,6 +518,8 @@ int bl_learned_features(bl_ctx *ctx, int n, const int *rowptr, const int *colids
   cudaFree(d_f);
   cudaFree(d_d);
   return rc;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 }  // extern "C"

@@ -647,7 +647,7 @@ int greedy_walk_run(bl_ctx *ctx, int batch, int iterations, double step0, double
 }  // namespace bl
 
 extern "C" int bl_greedy_walks(bl_ctx *ctx, long long *offsets, int *sources, int *counts, long long cap,
-                               long long *total) {
+                               long long *total) try {
   if (!ctx || !offsets || !total || cap < 0 || (cap > 0 && (!sources || !counts))) return BL_ERR_ARG;
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   if (int rc = bl::greedy_walks_build(ctx)) return rc;
@@ -664,4 +664,6 @@ extern "C" int bl_greedy_walks(bl_ctx *ctx, long long *offsets, int *sources, in
     }
   }
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }

@@ -236,7 +236,7 @@ extern "C" {
 
 int bl_learned_train(bl_ctx *ctx, int num_graphs, const int *vertex_offset, const long long *edge_offset,
                      const int *rowptr, const int *colids, const double *layouts, int epochs, double lr, int seed,
-                     float *params, double *scale_model, double *loss_history) {
+                     float *params, double *scale_model, double *loss_history) try {
   using namespace bl;
   if (!ctx || num_graphs < 1 || !vertex_offset || !edge_offset || !rowptr || !layouts || !params || !scale_model ||
       epochs < 0 || !(lr > 0))
@@ -406,9 +406,11 @@ int bl_learned_train(bl_ctx *ctx, int num_graphs, const int *vertex_offset, cons
   cudaFree(d_f);
   cudaFree(d_d);
   return rc;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_learned_load_model(const char *path, float *params, double *scale_model) {
+int bl_learned_load_model(const char *path, float *params, double *scale_model) try {
   if (!path || !params || !scale_model) return BL_ERR_ARG;
   FILE *f = std::fopen(path, "rb");
   if (!f) return BL_ERR_IO;
@@ -441,17 +443,21 @@ int bl_learned_load_model(const char *path, float *params, double *scale_model) 
   }
   std::fclose(f);
   return rc;
+} catch (...) {
+  return bl_host_exception(nullptr);
 }
 
-int bl_learned_init(bl_ctx *ctx, const float *params, const double *scale_model, int seed) {
+int bl_learned_init(bl_ctx *ctx, const float *params, const double *scale_model, int seed) try {
   if (!ctx || !params || !scale_model) return BL_ERR_ARG;
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   if (ctx->g.n < 2) return bl_fail(ctx, BL_ERR_STATE, "bl_learned_init needs a context with a graph");
   return bl::learned_init(ctx, params, scale_model, seed);
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 int bl_learned_layout(bl_ctx *ctx, const float *params, const double *scale_model, int seed, int max_iterations,
-                      int batch, double theta, double target_energy, double step0, double *out) {
+                      int batch, double theta, double target_energy, double step0, double *out) try {
   using namespace bl;
   if (!ctx || !params || !scale_model || !out || max_iterations < 1 || batch < 1 || !(theta > 0) || !(step0 > 0))
     return BL_ERR_ARG;
@@ -482,6 +488,8 @@ int bl_learned_layout(bl_ctx *ctx, const float *params, const double *scale_mode
   out[3] = fell_back;
   out[4] = t_init;
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 }  // extern "C"

@@ -618,7 +618,7 @@ unsigned char *g_noalloc_ptr[kMaxDevices] = {nullptr};
 extern "C" int bl_minibatch_iteration_noalloc(int n, const int *d_rowptr, const int *d_colids,
                                               float *d_xy, double *d_force, double *d_vertex_energy,
                                               int model, int batch, double weight, double step,
-                                              double *energy_out, void *stream) {
+                                              double *energy_out, void *stream) try {
   using namespace bl;
   if (n < 1 || !d_rowptr || !d_colids || !d_xy || !d_force || !d_vertex_energy)
     return BL_ERR_ARG;
@@ -708,4 +708,6 @@ extern "C" int bl_minibatch_iteration_noalloc(int n, const int *d_rowptr, const 
   if (host_status.code != DEV_OK) return BL_ERR_DEVICE_TIMEOUT;
   if (energy_out) *energy_out = host_energy;
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(nullptr);
 }

@@ -752,15 +752,17 @@ int mpnn_set_params_device(bl_ctx *ctx, const float *h_params) {
 // ---- C ABI -------------------------------------------------------------------------
 extern "C" {
 
-int bl_mpnn_set_params(bl_ctx *ctx, const float *params) {
+int bl_mpnn_set_params(bl_ctx *ctx, const float *params) try {
   if (!ctx || !params) return BL_ERR_ARG;
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   if (int rc = bl::mpnn_set_params_device(ctx, params)) return rc;
   BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
-int bl_mpnn_get_params(bl_ctx *ctx, float *params) {
+int bl_mpnn_get_params(bl_ctx *ctx, float *params) try {
   if (!ctx || !params) return BL_ERR_ARG;
   if (!ctx->mpnn || !ctx->mpnn->have_params) return bl_fail(ctx, BL_ERR_STATE, "no network parameters set");
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -768,6 +770,8 @@ int bl_mpnn_get_params(bl_ctx *ctx, float *params) {
                                ctx->stream));
   BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return BL_OK;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 // Forward (and, with target != NULL, loss and gradient) on a graph given as
@@ -775,7 +779,7 @@ int bl_mpnn_get_params(bl_ctx *ctx, float *params) {
 // uint16), loss and grad (kMpnnParams floats).
 int bl_mpnn_run(bl_ctx *ctx, int n, const int *rowptr, const int *colids, const float *features,
                 const float *target, const float *vweight, float *xy, unsigned short *h, double *loss,
-                float *grad) {
+                float *grad) try {
   using namespace bl;
   if (!ctx || n < 1 || !rowptr || !features || !xy) return BL_ERR_ARG;
   if (target && (!vweight || !loss || !grad)) return bl_fail(ctx, BL_ERR_ARG, "training run needs vweight, loss, grad");
@@ -828,6 +832,8 @@ int bl_mpnn_run(bl_ctx *ctx, int n, const int *rowptr, const int *colids, const 
   cudaFree(d_ci);
   cudaFree(d_f);
   return rc;
+} catch (...) {
+  return bl_host_exception(ctx);
 }
 
 }  // extern "C"

@@ -35,6 +35,7 @@ extern "C" {
 #define BL_ERR_TOO_LARGE (-5)      /* problem exceeds a documented limit    */
 #define BL_ERR_IO (-6)             /* file could not be read or written     */
 #define BL_ERR_STATE (-7)          /* call order violated (e.g. no graph)   */
+#define BL_ERR_HOST (-8)           /* host-side failure (memory, threads)   */
 
 typedef struct bl_ctx bl_ctx;
 

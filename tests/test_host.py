@@ -533,3 +533,32 @@ def test_kernels_do_not_spill(L):
         if spill > allowed:
             bad.append((k, spill))
     assert not bad, bad
+
+
+EXC_CHILD = r"""
+import ctypes as C, resource, sys
+lib = C.CDLL(sys.argv[1])
+vm = 0
+for line in open("/proc/self/status"):
+    if line.startswith("VmSize:"):
+        vm = int(line.split()[1]) * 1024
+resource.setrlimit(resource.RLIMIT_AS, (vm + (1 << 30), resource.RLIM_INFINITY))
+buf = (C.c_double * 4)(7, 7, 7, 7)
+rc = lib.bl_random_coordinates((1 << 30) - 1, buf)        # 16 GB of host vector: bad_alloc
+print(rc, list(buf))
+"""
+
+
+def test_host_exceptions_do_not_cross_the_abi(L, tmp_path):
+    """A host allocation that fails inside an entry point comes back as
+    BL_ERR_HOST (-8) instead of aborting the caller: a child process caps its
+    address space and asks for a start of 2^30 - 1 vertices."""
+    import sys
+    src = tmp_path / "exc.py"
+    src.write_text(EXC_CHILD)
+    lib = os.path.join(ROOT, "batchlayoutcode_gb300", "_build", "libbatchlayout_gb300.so")
+    r = subprocess.run([sys.executable, str(src), lib], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    rc, buf = r.stdout.split(" ", 1)
+    assert int(rc) == -8
+    assert buf.strip() == "[7.0, 7.0, 7.0, 7.0]"  # nothing written
