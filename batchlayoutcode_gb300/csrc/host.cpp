@@ -396,6 +396,31 @@ struct CacheHeader {
   int symmetric, pad;
 };
 
+// rowptr non-decreasing from 0 to colids.size(), every colid in [0, cols):
+// checked in parallel slices of rows.
+bool csr_consistent(const std::vector<int> &rowptr, const std::vector<int> &colids, int cols) {
+  const int rows = (int)rowptr.size() - 1;
+  if (rows < 0 || rowptr[0] != 0 || (size_t)rowptr[rows] != colids.size()) return false;
+  const int T = host_threads(colids.size() + (size_t)rows, 1 << 20);
+  std::vector<char> good(T, 1);
+  parallel_for(T, [&](int k) {
+    const int lo = (int)((long long)rows * k / T), hi = (int)((long long)rows * (k + 1) / T);
+    for (int i = lo; i < hi; i++)
+      if (rowptr[i + 1] < rowptr[i]) {
+        good[k] = 0;
+        return;
+      }
+    for (int e = rowptr[lo]; e < rowptr[hi]; e++)
+      if (colids[e] < 0 || colids[e] >= cols) {
+        good[k] = 0;
+        return;
+      }
+  });
+  for (char g : good)
+    if (!g) return false;
+  return true;
+}
+
 bool source_stamp(const std::string &path, long long &size, long long &mtime_ns) {
   struct stat st;
   if (stat(path.c_str(), &st) != 0) return false;
@@ -425,14 +450,20 @@ bool read_matrix_market_cached(const std::string &path, const std::string &cache
   if (stamped) {
     if (FILE *f = std::fopen(cpath.c_str(), "rb")) {
       CacheHeader h;
+      struct stat cst;
+      // the header's sizes must account for the file's length exactly before
+      // anything is sized from them; the arrays are checked after the read,
+      // and a cache that fails either check is parsed again and rewritten
       bool ok = std::fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, kCacheMagic, 8) == 0 &&
-                h.src_size == size && h.src_mtime_ns == mtime && h.rows >= 0 && h.nnz >= 0;
+                h.src_size == size && h.src_mtime_ns == mtime && h.rows >= 0 && h.cols >= 0 && h.nnz >= 0 &&
+                h.nnz <= 2147483647LL && fstat(fileno(f), &cst) == 0 &&
+                (long long)cst.st_size == (long long)sizeof(h) + 4LL * ((long long)h.rows + 1) + 4LL * h.nnz;
       if (ok) {
         rowptr.assign((size_t)h.rows + 1, 0);
         colids.assign((size_t)h.nnz, 0);
         ok = std::fread(rowptr.data(), sizeof(int), rowptr.size(), f) == rowptr.size() &&
              (h.nnz == 0 || std::fread(colids.data(), sizeof(int), colids.size(), f) == colids.size()) &&
-             rowptr[0] == 0 && rowptr[h.rows] == h.nnz;
+             csr_consistent(rowptr, colids, h.cols);
       }
       std::fclose(f);
       if (ok) {

@@ -264,6 +264,44 @@ def test_reader_binary_cache(L, tmp_path):
     assert not i4["cached"] and rp4.tolist() == [0, 1, 1, 2]
 
 
+@pytest.mark.parametrize("damage", ["truncated", "rows", "huge_nnz", "colid", "rowptr", "magic"])
+def test_reader_binary_cache_damaged(L, tmp_path, damage):
+    """A cache file whose stamp still matches the source but whose contents
+    are damaged is not trusted: the header's sizes must match the file's
+    length before anything is allocated from them, the CSR must be
+    consistent after the read; otherwise the text is parsed again and the
+    cache rewritten."""
+    import struct
+    src = tmp_path / "g.mtx"
+    src.write_text(open(os.path.join(GOLDEN, "rgg.mtx")).read())
+    cache = tmp_path / "cache"
+    cache.mkdir()
+    rp0, ci0, _ = L.read_matrix_market(str(src))
+    L.read_matrix_market(str(src), str(cache))
+    f = cache / "g.mtx.blcsr"
+    b = bytearray(f.read_bytes())
+    hdr = 48  # magic, source size, source mtime, rows, cols, nnz, symmetric, pad
+    rows = struct.unpack_from("<i", b, 24)[0]
+    if damage == "truncated":
+        b = b[:-4]
+    elif damage == "rows":
+        struct.pack_into("<i", b, 24, rows + 1)
+    elif damage == "huge_nnz":
+        struct.pack_into("<q", b, 32, 1 << 40)
+    elif damage == "colid":
+        struct.pack_into("<i", b, hdr + 4 * (rows + 1) + 40, 10 ** 9)
+    elif damage == "rowptr":
+        struct.pack_into("<i", b, hdr + 4 * 5, 10 ** 6)
+    elif damage == "magic":
+        b[0] ^= 0xFF
+    f.write_bytes(bytes(b))
+    rp, ci, info = L.read_matrix_market(str(src), str(cache))
+    assert not info["cached"]
+    assert np.array_equal(rp, rp0) and np.array_equal(ci, ci0)
+    rp, ci, info = L.read_matrix_market(str(src), str(cache))  # rewritten
+    assert info["cached"] and np.array_equal(rp, rp0) and np.array_equal(ci, ci0)
+
+
 def test_writer_parallel_slices(L, tmp_path):
     rng = np.random.default_rng(3)
     xy = rng.normal(0, 100, (300000, 2)) * rng.choice([1e-6, 1.0, 1e6], (300000, 2))
