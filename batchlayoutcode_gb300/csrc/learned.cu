@@ -442,6 +442,11 @@ int bl_learned_load_model(const char *path, float *params, double *scale_model) 
     std::memcpy(&scale_model[i], &u, 8);
   }
   std::fclose(f);
+  // a non-finite weight or scale would give a start of NaNs: not a model
+  for (int i = 0; i < bl::kMpnnParams && !rc; i++)
+    if (!std::isfinite(params[i])) rc = BL_ERR_IO;
+  for (int i = 0; i < 3 && !rc; i++)
+    if (!std::isfinite(scale_model[i])) rc = BL_ERR_IO;
   return rc;
 } catch (...) {
   return bl_host_exception(nullptr);

@@ -29,6 +29,18 @@ def test_model_file_round_trip(tmp_path):
         f.write(b"NOTAMODEL" + bytes(16))
     assert L.bl_learned_load_model(bad.encode(), p3.ctypes.data_as(C.POINTER(C.c_float)),
                                    sm3.ctypes.data_as(C.POINTER(C.c_double))) == -6
+    # truncated, and non-finite weights or scales: rejected as not a model
+    with open(path, "rb") as f:
+        good = f.read()
+    with open(bad, "wb") as f:
+        f.write(good[:-5])
+    assert L.bl_learned_load_model(bad.encode(), p3.ctypes.data_as(C.POINTER(C.c_float)),
+                                   sm3.ctypes.data_as(C.POINTER(C.c_double))) == -6
+    for pn, smn in ((np.where(np.arange(LR.MPNN_PARAMS) == 17, np.nan, p).astype(np.float32), sm),
+                    (p, np.array([1.5, np.inf, 3.0]))):
+        LR.save_model(bad, pn, smn)
+        assert L.bl_learned_load_model(bad.encode(), p3.ctypes.data_as(C.POINTER(C.c_float)),
+                                       sm3.ctypes.data_as(C.POINTER(C.c_double))) == -6
 
 
 def test_shipped_model_loads():
