@@ -355,6 +355,30 @@ def test_cli_help_and_missing_input():
     assert r.returncode == 1 and "-input <string>" in r.stdout
 
 
+def test_cli_stdout_before_the_layout_matches_reference(L, tmp_path):
+    """The 16 lines the CLI prints before the layout (banner, reader lines,
+    matrix sizes) equal the reference binary's, as recorded in the golden
+    stdout, up to the input path and the parse time: the wrapper reads the
+    wall time and output path by line index (runBatchLayout.py:55-56), so
+    the count and order of these lines matter.  Without a GPU the run stops
+    after them at context creation."""
+    r = subprocess.run([cli(), "-input", os.path.join(GOLDEN, "grid12.mtx"), "-output", str(tmp_path) + "/",
+                        "-algo", "2", "-iter", "1", "-batch", "32"],
+                       capture_output=True, text=True, cwd=str(tmp_path), timeout=300)
+    assert r.returncode in (0, 2), r.stderr
+    ref = open(os.path.join(GOLDEN, "ref_stdout_grid12.txt")).read().split("\n")[:16]
+
+    def norm(lines):
+        out = []
+        for line in lines:
+            line = re.sub(r"^Input File Directory:.*grid12\.mtx$", "Input File Directory:grid12.mtx", line)
+            line = re.sub(r"format: \S+ seconds$", "format: T seconds", line)
+            out.append(line)
+        return out
+
+    assert norm(r.stdout.split("\n")[:16]) == norm(ref)
+
+
 def test_cli_rejects_algorithms_off_the_gpu_path(tmp_path):
     for algo in (0, 1):
         r = subprocess.run([cli(), "-input", os.path.join(GOLDEN, "grid12.mtx"), "-algo", str(algo)],
