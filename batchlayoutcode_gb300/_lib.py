@@ -29,6 +29,7 @@ EXPORTS = (
     "bl_learned_features", "bl_learned_train", "bl_learned_init", "bl_learned_layout",
     "bl_learned_load_model", "bl_approx_force_directed", "bl_cache_blocking_minibatch_sd",
     "bl_greedy_iteration", "bl_greedy_walks", "bl_read_matrix_market_cached", "bl_bfs_init",
+    "bl_cursor_neighbours",
 )
 
 _lib = None
@@ -111,6 +112,7 @@ def load() -> C.CDLL:
         "bl_greedy_iteration": (i32, [vp, i32, f64, dp]),
         "bl_greedy_walks": (i32, [vp, C.POINTER(C.c_longlong), ip, ip, i64, C.POINTER(C.c_longlong)]),
         "bl_bfs_init": (i32, [vp]),
+        "bl_cursor_neighbours": (i32, [i32, ip, ip, ip, ip]),
         "bl_read_matrix_market_cached": (i32, [cp, cp, C.POINTER(C.c_longlong), dp, C.POINTER(ip), C.POINTER(ip),
                                                cp, i32]),
     }
@@ -175,6 +177,24 @@ def greedy_coordinates(rowptr, colids) -> np.ndarray:
     if rc != 0:
         raise BatchLayoutError(rc, "bl_greedy_coordinates")
     return out
+
+
+def cursor_neighbours(rowptr, colids):
+    """The neighbour lists the reference's kindex cursor matches, host only:
+    -> (matched_rowptr, matched_colids)."""
+    rp = np.ascontiguousarray(rowptr, dtype=np.int32)
+    ci = np.ascontiguousarray(colids, dtype=np.int32)
+    n = rp.shape[0] - 1
+    L = load()
+    mrp = np.zeros(n + 1, dtype=np.int32)
+    rc = L.bl_cursor_neighbours(n, _ip(rp), _ip(ci), _ip(mrp), None)
+    if rc != 0:
+        raise BatchLayoutError(rc, "bl_cursor_neighbours")
+    mci = np.zeros(max(int(mrp[-1]), 1), dtype=np.int32)
+    rc = L.bl_cursor_neighbours(n, _ip(rp), _ip(ci), _ip(mrp), _ip(mci))
+    if rc != 0:
+        raise BatchLayoutError(rc, "bl_cursor_neighbours")
+    return mrp, mci[:int(mrp[-1])]
 
 
 def write_coordinates(input: str, outputdir: str, tag: str, xy) -> str:

@@ -482,6 +482,18 @@ int bl_greedy_coordinates(int n, const int *rowptr, const int *colids, double *x
   return bl_host_exception(nullptr);
 }
 
+int bl_cursor_neighbours(int n, const int *rowptr, const int *colids, int *matched_rowptr, int *matched_colids) try {
+  if (!rowptr || !colids || !matched_rowptr || n < 1 || n > kMaxVertices || csr_error(n, rowptr[n], rowptr, colids))
+    return BL_ERR_ARG;
+  std::vector<int> rp(rowptr, rowptr + n + 1), ci(colids, colids + rowptr[n]), erp, eci;
+  bl::cursor_neighbours(n, rp, ci, erp, eci);
+  std::memcpy(matched_rowptr, erp.data(), erp.size() * sizeof(int));
+  if (matched_colids && !eci.empty()) std::memcpy(matched_colids, eci.data(), eci.size() * sizeof(int));
+  return BL_OK;
+} catch (...) {
+  return bl_host_exception(nullptr);
+}
+
 int bl_write_coordinates(const char *input, const char *outputdir, const char *tag, const double *xy,
                          int n, char *path_out, int path_cap) try {
   if (!input || !outputdir || !tag || (n > 0 && !xy)) return BL_ERR_ARG;

@@ -385,8 +385,12 @@ bool read_matrix_market(const std::string &path, MatrixInfo &info, std::vector<i
 // ---- binary CSR cache ---------------------------------------------------------
 
 namespace {
-constexpr char kCacheMagic[8] = {'B', 'L', 'C', 'S', 'R', '0', '0', '1'};
+constexpr char kCacheMagic[8] = {'B', 'L', 'C', 'S', 'R', '0', '0', '2'};
 
+// The header is followed by the source's canonical absolute path (path_len
+// bytes, zero-padded to a multiple of 8), then rowptr and colids.  A cache is
+// used only for the file it was made from: same canonical path, device and
+// inode, size and modification time.
 struct CacheHeader {
   char magic[8];
   long long src_size;
@@ -394,6 +398,13 @@ struct CacheHeader {
   int rows, cols;
   long long nnz;
   int symmetric, pad;
+  long long src_dev, src_ino;
+  int path_len, pad2;
+};
+
+struct SourceStamp {
+  long long size = 0, mtime_ns = 0, dev = 0, ino = 0;
+  std::string canon;  // realpath of the source
 };
 
 // rowptr non-decreasing from 0 to colids.size(), every colid in [0, cols):
@@ -421,13 +432,21 @@ bool csr_consistent(const std::vector<int> &rowptr, const std::vector<int> &coli
   return true;
 }
 
-bool source_stamp(const std::string &path, long long &size, long long &mtime_ns) {
+bool source_stamp(const std::string &path, SourceStamp &s) {
   struct stat st;
   if (stat(path.c_str(), &st) != 0) return false;
-  size = (long long)st.st_size;
-  mtime_ns = (long long)st.st_mtim.tv_sec * 1000000000LL + (long long)st.st_mtim.tv_nsec;
-  return true;
+  s.size = (long long)st.st_size;
+  s.mtime_ns = (long long)st.st_mtim.tv_sec * 1000000000LL + (long long)st.st_mtim.tv_nsec;
+  s.dev = (long long)st.st_dev;
+  s.ino = (long long)st.st_ino;
+  char *rp = realpath(path.c_str(), nullptr);
+  if (!rp) return false;
+  s.canon = rp;
+  std::free(rp);
+  return s.canon.size() < 65536;
 }
+
+long long padded_path_bytes(long long len) { return (len + 7) & ~7LL; }
 }  // namespace
 
 std::string csr_cache_path(const std::string &path, const std::string &cache_dir) {
@@ -444,9 +463,10 @@ bool read_matrix_market_cached(const std::string &path, const std::string &cache
                                bool *from_cache) {
   const auto t0 = std::chrono::steady_clock::now();
   if (from_cache) *from_cache = false;
-  long long size = 0, mtime = 0;
-  const bool stamped = source_stamp(path, size, mtime);
+  SourceStamp src;
+  const bool stamped = source_stamp(path, src);
   const std::string cpath = csr_cache_path(path, cache_dir);
+  const long long plen = (long long)src.canon.size();
   if (stamped) {
     if (FILE *f = std::fopen(cpath.c_str(), "rb")) {
       CacheHeader h;
@@ -455,9 +475,16 @@ bool read_matrix_market_cached(const std::string &path, const std::string &cache
       // anything is sized from them; the arrays are checked after the read,
       // and a cache that fails either check is parsed again and rewritten
       bool ok = std::fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, kCacheMagic, 8) == 0 &&
-                h.src_size == size && h.src_mtime_ns == mtime && h.rows >= 0 && h.cols >= 0 && h.nnz >= 0 &&
+                h.src_size == src.size && h.src_mtime_ns == src.mtime_ns && h.src_dev == src.dev &&
+                h.src_ino == src.ino && h.path_len == plen && h.rows >= 0 && h.cols >= 0 && h.nnz >= 0 &&
                 h.nnz <= 2147483647LL && fstat(fileno(f), &cst) == 0 &&
-                (long long)cst.st_size == (long long)sizeof(h) + 4LL * ((long long)h.rows + 1) + 4LL * h.nnz;
+                (long long)cst.st_size == (long long)sizeof(h) + padded_path_bytes(plen) +
+                                              4LL * ((long long)h.rows + 1) + 4LL * h.nnz;
+      if (ok) {
+        std::string stored((size_t)padded_path_bytes(plen), '\0');
+        ok = std::fread(&stored[0], 1, stored.size(), f) == stored.size() &&
+             std::memcmp(stored.data(), src.canon.data(), (size_t)plen) == 0;
+      }
       if (ok) {
         rowptr.assign((size_t)h.rows + 1, 0);
         colids.assign((size_t)h.nnz, 0);
@@ -485,13 +512,19 @@ bool read_matrix_market_cached(const std::string &path, const std::string &cache
       CacheHeader h;
       std::memset(&h, 0, sizeof(h));
       std::memcpy(h.magic, kCacheMagic, 8);
-      h.src_size = size;
-      h.src_mtime_ns = mtime;
+      h.src_size = src.size;
+      h.src_mtime_ns = src.mtime_ns;
       h.rows = info.rows;
       h.cols = info.cols;
       h.nnz = info.nnz;
       h.symmetric = info.symmetric ? 1 : 0;
+      h.src_dev = src.dev;
+      h.src_ino = src.ino;
+      h.path_len = (int)plen;
+      std::string stored((size_t)padded_path_bytes(plen), '\0');
+      std::memcpy(&stored[0], src.canon.data(), (size_t)plen);
       bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 &&
+                std::fwrite(stored.data(), 1, stored.size(), f) == stored.size() &&
                 std::fwrite(rowptr.data(), sizeof(int), rowptr.size(), f) == rowptr.size() &&
                 (colids.empty() || std::fwrite(colids.data(), sizeof(int), colids.size(), f) == colids.size());
       ok = (std::fclose(f) == 0) && ok;

@@ -53,8 +53,9 @@ bool read_matrix_market(const std::string &path, MatrixInfo &info, std::vector<i
                         std::vector<int> &colids, std::string &msg);
 
 // The same CSR through a binary cache: <cache_dir>/<basename>.blcsr holds the
-// CSR and the source file's size and modification time; a cache that matches
-// the source is read instead of the text (no parsing), otherwise the text is
+// CSR and the source file's canonical absolute path, device, inode, size and
+// modification time; a cache made from this very file, unchanged, is read
+// instead of the text (no parsing), otherwise the text is
 // parsed and the cache (re)written (write failures are ignored).
 // *from_cache (may be null) tells which happened.
 bool read_matrix_market_cached(const std::string &path, const std::string &cache_dir, MatrixInfo &info,

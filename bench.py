@@ -14,8 +14,12 @@ value      device-resident throughput: n * K / (sum of CUDA-event times of the
 e2e        the same through the C ABI with host buffers: per step, copy the
            coordinates from pinned host memory, run the iteration, copy them
            back (host wall clock).
-roofline   dominant kernel (the repulsion traversal): algorithmic bytes =
-           node-record visits x 16 B per launch, over its CUDA-event time.
+roofline   dominant kernel (the repulsion traversal), bound by instruction
+           issue: warp instructions per launch (live record visits x the
+           instructions per visit of its committed ncu capture) over
+           152 SMs x 4 schedulers x the sampled SM clock; beside it the
+           step's algorithmic bytes (build, traversal, sweep) over the step
+           time against the measured HBM copy bandwidth.
 cpu_baseline  the FP64 oracle port (reference Makefile optimisation flags)
            on all host cores, a bounded sample of iterations from the same start.
 
@@ -68,6 +72,10 @@ WORKLOADS = {
                              "and algo 4 (bht 1.2) from there, batch 256; one persistent launch replayed as a "
                              "CUDA graph"),
 }
+REF_BINARY_NOTE = ("the reference binary (oracle/_ref/BatchLayout, built from the reference's sources with its "
+                   "Makefile flags) is an x86-64 build that does not travel to this Arm host and the reference "
+                   "sources are not here to rebuild it; the port restates the same FP64 arithmetic and is pinned "
+                   "bit-exact to the reference (strict flags) by the golden-vector tests")
 KERNEL_FOR_ALGO = {4: "traverse_kernel", 2: "minibatch_kernel", 3: "minibatch_kernel", 8: "minibatch_kernel",
                    7: "minibatch_kernel", 5: "greedy_iteration_kernel"}
 DECAY = {2: 0.999, 4: 0.999, 7: 0.999, 3: 0.99, 8: 0.99, 5: 0.99}
@@ -158,31 +166,97 @@ def peaks():
 
 def traffic_from_profile(kernel: str, workload: str):
     """dram bytes per launch from the committed ncu summary, if there is one."""
+    return profile_figure(kernel, workload, "dram_bytes_per_launch")
+
+
+def profile_figure(kernel: str, workload: str, key: str):
+    """A `key: value` figure from the committed ncu summary of the kernel."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     if not os.path.exists(path):
         return None
-    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+    m = re.search(re.escape(key) + r":\s*([0-9.eE+]+)", open(path).read())
     return float(m.group(1)) if m else None
 
 
-def l2_bandwidth_gbs(torch, device: int) -> float:
-    """Read+write bandwidth of an L2-resident copy (2 x 24 MB buffers, well
-    inside the 129 MB L2), CUDA events, best of 5: the ceiling for kernels
-    whose working set stays in L2."""
-    n = 24 * 1024 * 1024 // 4
-    a = torch.empty(n, dtype=torch.float32, device=f"cuda:{device}").fill_(1.0)
-    b = torch.empty_like(a)
-    best = 0.0
-    for _ in range(5):
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record()
-        for _ in range(20):
-            b.copy_(a)
-            a.copy_(b)
-        e.record()
-        e.synchronize()
-        best = max(best, 40 * 2 * a.numel() * 4 / (s.elapsed_time(e) * 1e-3) / 1e9)
-    return best
+def allpairs_fraction(B, torch, device: int, flush, iterations: int = 3) -> dict:
+    """All-pairs minibatch (algo 2) on the 100,000-vertex Chung-Lu graph: the
+    minibatch kernel's time per iteration (CUDA events on the library's
+    stream, L2 flushed before each iteration) and its fraction of the FP32
+    FMA peak (10 flops per ordered pair, n^2 pairs per iteration)."""
+    g, xy = load_workload("chunglu100k")
+    with B.Algorithms(g.rowptr, g.colids, device=device) as a:
+        a.nCoordinates = xy
+        a.run_resident(2, 1, 256, 1.2, 1.0, want_energy=True)  # warm-up (builds the cursor table)
+        a.kernel_time("minibatch_kernel")
+        step = 0.999
+        for _ in range(iterations):
+            flush.zero_()
+            torch.cuda.synchronize()
+            a.run_resident(2, 1, 256, 1.2, step, want_energy=True)
+            step *= 0.999
+        torch.cuda.synchronize()
+        ms, cnt = a.kernel_time()
+    per_it = ms / max(cnt, 1)
+    flops = 10.0 * float(g.n) * g.n
+    peak = 152 * 128 * 2 * 2070e6 / 1e12
+    tflops = flops / (per_it * 1e-3) / 1e12
+    return {"workload": "chunglu100k: " + WORKLOADS["chunglu100k"]["desc"], "vertices": g.n,
+            "ms_per_iteration": per_it, "iterations": cnt, "tflops": tflops, "peak_tflops": peak,
+            "frac": tflops / peak,
+            "pairs_per_clock_per_sm": float(g.n) * g.n / (per_it * 1e-3) / 152 / 2070e6,
+            "note": "minibatch_kernel per iteration; peak = nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 "
+                    "flops x 2,070 MHz; the kernel's reciprocal (one MUFU operation per pair at 16 per clock "
+                    "per SM) caps it at 16 pairs per clock per SM, 0.625 of this peak"}
+
+
+def bh_roofline(g, kernel, workload, visits, kernel_s, step_s, sm_mhz, pk):
+    """Roofline of the Barnes-Hut traversal and of the whole step.
+
+    The traversal reads its tree records from L1/L2 (about 4 % of the record
+    bytes reach DRAM), so its bound is instruction issue: warp instructions
+    per launch = live record visits x (warp instructions per visit of the
+    committed ncu capture of this kernel), over 152 SMs x 4 schedulers x the
+    median SM clock sampled during the timed steps.  The record bytes (16 B
+    per visit) are kept as a labelled secondary figure, and the step's
+    algorithmic bytes (tree build, traversal, level sweep) over the step time
+    give the HBM fraction of the whole iteration."""
+    hbm = pk["hbm_gbs"] if pk else 6800.0
+    hbm_src = "measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "fallback 6.8 TB/s"
+    inst_prof = profile_figure(kernel, workload, "warp_instructions_per_launch")
+    visits_prof = profile_figure(kernel, workload, "record_visits_per_launch")
+    n, nnz = float(g.n), float(g.nnz)
+    # per iteration: Morton keys (read 8 B, write 8 B), 4 LSD passes over
+    # (key 8 B + vertex 4 B) read and written, sorted positions and tree nodes
+    # (~2n nodes of 24 B), pre-order records (2n x 16 B + FP64 centroid 16 B)
+    build = n * 16 + 4 * n * 24 + n * 8 + 2 * n * 24 + 2 * n * 32
+    traversal = visits * 16.0 + nnz * 12 + n * 24
+    sweep = n * 24 + nnz * 12
+    step_bytes = build + traversal + sweep
+    step = {"bound": "hbm", "achieved": step_bytes / step_s / 1e9, "peak": hbm, "unit": "GB/s",
+            "frac": step_bytes / step_s / 1e9 / hbm, "algorithmic_bytes_per_step": step_bytes,
+            "parts": {"build": build, "traversal": traversal, "sweep": sweep},
+            "note": "tree build + traversal (record visits x 16 B + CSR term) + level sweep, over ms_per_step; "
+                    "peak " + hbm_src}
+    records = {"achieved": visits * 16.0 / kernel_s / 1e9, "unit": "GB/s", "bytes_per_launch": visits * 16.0,
+               "frac_of_hbm": visits * 16.0 / kernel_s / 1e9 / hbm,
+               "note": "record visits x 16 B per launch over the traversal time; ~96 % of these bytes hit "
+                       "L1/L2, so this is not a DRAM figure"}
+    if inst_prof and visits_prof:
+        inst = visits * inst_prof / visits_prof
+        peak = 152 * 4 * sm_mhz * 1e6 / 1e9
+        return {"bound": "issue", "achieved": inst / kernel_s / 1e9, "peak": peak, "unit": "Gwarp-inst/s",
+                "frac": inst / kernel_s / 1e9 / peak, "traffic": traffic_from_profile(kernel, workload),
+                "kernel": kernel, "kernel_ms_per_launch": kernel_s * 1e3, "record_visits_per_launch": visits,
+                "warp_instructions_per_launch": inst,
+                "instructions_source": f"live record visits x {inst_prof / visits_prof:.4f} warp instructions per "
+                                       f"visit (smsp__inst_executed.sum / visits of the ncu capture in "
+                                       f"profiles/{kernel}_{workload}.md)",
+                "peak_source": f"152 SMs x 4 schedulers x 1 warp instruction per clock x {sm_mhz:.0f} MHz "
+                               "(median SM clock sampled during the timed steps)",
+                "record_bytes": records, "step": step}
+    return {"bound": "hbm", "achieved": step["achieved"], "peak": hbm, "unit": "GB/s", "frac": step["frac"],
+            "traffic": traffic_from_profile(kernel, workload), "kernel": "whole step", "record_bytes": records,
+            "step": step, "peak_source": hbm_src}
 
 
 def load_workload(name: str):
@@ -256,6 +330,15 @@ def baseline_iters(w, n):
     return max(1, min(600, int(2.0e11 / max(n * n, 1))))
 
 
+def workload_config(args, w, g) -> dict:
+    """The `config` object of both arms' lines (the same keys and values, so
+    that the two lines describe one workload)."""
+    ips = w.get("iters_per_step", 1)
+    return {"workload": f"{args.workload}: {w['desc']}", "vertices": g.n, "edges": g.nnz // 2,
+            "step": (f"{ips} layout iterations" if ips > 1 else "one layout iteration") + " over the whole graph",
+            "l2": "GPU steps: L2 flushed before every timed step (256 MB write)"}
+
+
 def run_reference(args, w, g, xy):
     """Reference CPU implementation on the same workload."""
     cores = os.cpu_count() or 1
@@ -296,8 +379,10 @@ def run_reference(args, w, g, xy):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"{args.workload}: {w['desc']}"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+            "config": workload_config(args, w, g),
+            "parallelism": f"host CPU, {cores} threads",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample,
+                             "why_port": None if kind == "reference" else REF_BINARY_NOTE},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -379,10 +464,23 @@ def run_reference_batched(args, w):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"{args.workload}: {w['desc']}"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+            "config": batched_config(args, w, graphs, algo),
+            "parallelism": f"host CPU, {cores} threads",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample,
+                             "why_port": None if kind == "reference" else REF_BINARY_NOTE},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def batched_config(args, w, graphs, algo) -> dict:
+    import numpy as np
+    algo = np.asarray(algo)
+    small = algo != 4
+    return {"workload": f"{args.workload}: {w['desc']}", "graphs": len(graphs),
+            "vertices": int(sum(len(rp) - 1 for rp, _ in graphs)),
+            "minibatch_graphs": int(small.sum()), "barnes_hut_graphs": int((~small).sum()),
+            "step": f"one batched layout: {w['iterations']} iterations of every graph",
+            "l2": "GPU steps: L2 flushed before every timed step (256 MB write)"}
 
 
 def run_batched(args, w, ws, rank, local):
@@ -485,18 +583,15 @@ def run_batched(args, w, ws, rank, local):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"{args.workload}: {w['desc']}", "graphs": len(sizes), "vertices": nv,
-                       "minibatch_graphs": int(small.sum()), "barnes_hut_graphs": int((~small).sum()),
-                       "step": f"one batched layout: {iters} iterations of every graph",
-                       "l2": "flushed before every timed step (256 MB write)",
-                       "autotuned_parts": bl.parts().tolist(),
-                       "block_ms": {"max_minibatch_graph": float(cyc[small].max() / sm_mhz / 1e3),
-                                    "max_barnes_hut_graph": float(cyc[~small].max() / sm_mhz / 1e3)
-                                    if (~small).any() else 0.0,
-                                    "sum_minibatch": float(cyc[small].sum() / sm_mhz / 1e3),
-                                    "sum_barnes_hut": float(cyc[~small].sum() / sm_mhz / 1e3),
-                                    "note": "clock64 cycles per graph / max SM clock"},
-                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "config": batched_config(args, w, graphs, algo),
+            "parallelism": "replicas" if ws > 1 else "single GPU",
+            "autotuned_parts": bl.parts().tolist(),
+            "block_ms": {"max_minibatch_graph": float(cyc[small].max() / sm_mhz / 1e3),
+                         "max_barnes_hut_graph": float(cyc[~small].max() / sm_mhz / 1e3)
+                         if (~small).any() else 0.0,
+                         "sum_minibatch": float(cyc[small].sum() / sm_mhz / 1e3),
+                         "sum_barnes_hut": float(cyc[~small].sum() / sm_mhz / 1e3),
+                         "note": "clock64 cycles per graph / max SM clock"},
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
@@ -609,6 +704,8 @@ def main():
     ap.add_argument("--workload", default="rgg1m", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-allpairs", action="store_true",
+                    help="skip the all-pairs minibatch figure on the 100k Chung-Lu graph in the default line")
     ap.add_argument("--stages", action="store_true",
                     help="Barnes-Hut workloads: print the live time of every stage of one iteration and exit")
     ap.add_argument("--io", action="store_true",
@@ -718,19 +815,9 @@ def main():
     if algo == 4:
         _, (visits_after, _) = a.bh_repulsion(theta)
         visits = 0.5 * (visits_before + visits_after)
-        alg_bytes = visits * 16.0
         avg_s = kern_ms / max(kern_count, 1) / 1e3
-        achieved = alg_bytes / avg_s / 1e9
-        peak = pk["hbm_gbs"] if pk else 6800.0
-        l2 = l2_bandwidth_gbs(torch, device)
-        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic_from_profile(kernel, args.workload),
-                "kernel": kernel, "kernel_ms_per_launch": avg_s * 1e3, "launches": kern_count,
-                "algorithmic_bytes_per_launch": alg_bytes,
-                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "fallback",
-                "l2": {"peak": l2, "frac": achieved / l2,
-                       "note": "the tree records are read from L1/L2; peak = L2-resident copy bandwidth "
-                               "measured in this run"}}
+        sm_mhz = (clocks or {}).get("sm_mhz") or (pk or {}).get("sm_max_mhz", 2070.0)
+        roof = bh_roofline(g, kernel, args.workload, visits, avg_s, total_ms / args.steps / 1e3, sm_mhz, pk)
     elif algo == 5:
         # per first-phase iteration and vertex: rowptr (8 B), walk offsets
         # (16 B), own position (8 B), force write + read (32 B), position
@@ -766,6 +853,9 @@ def main():
     tte = None
     if algo == 4 and rank == 0 and not args.no_learned:
         tte = time_to_energy(B, g, w)
+    allpairs = None
+    if algo == 4 and rank == 0 and not args.no_allpairs:
+        allpairs = allpairs_fraction(B, torch, device, flush)
 
     # end to end through the C ABI with pinned host buffers: every step copies
     # its input coordinates in and its result out (the two buffers take turns)
@@ -792,15 +882,12 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"{args.workload}: {w['desc']}", "vertices": g.n, "edges": g.nnz // 2,
-                       "step": (f"{ips} layout iterations" if ips > 1 else "one layout iteration") +
-                               " over the whole graph" +
-                               (f" (replay of the captured iteration, a CUDA graph of its {launches // args.steps} "
-                                "kernel launches)" if graph else ""),
-                       "l2": "flushed before every timed step (256 MB write)",
-                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "config": workload_config(args, w, g),
+            "parallelism": "replicas" if ws > 1 else "single GPU",
+            "step_launch": (f"replay of the captured iteration, a CUDA graph of its {launches // args.steps} "
+                            "kernel launches") if graph else "direct launches",
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-            "time_to_energy": tte,
+            "time_to_energy": tte, "allpairs_chunglu100k": allpairs,
         }
         print(json.dumps(line), flush=True)
     a.close()

@@ -70,7 +70,8 @@ int bl_read_matrix_market(const char *path, long long *info, double *seconds, in
                           int **colids, char *err, int errcap);
 /* The same through a binary CSR cache (no reference counterpart): with
  * cache_dir not NULL, <cache_dir>/<basename(path)>.blcsr is read instead of
- * the text when it records the text file's current size and modification
+ * the text when it was made from this very file (same canonical absolute
+ * path, device and inode) and records its current size and modification
  * time, else the text is parsed and the cache written (a failed write is
  * ignored).  info[4] = 1 when the cache was used, else 0 (info holds 5
  * values); seconds = load time. */
@@ -111,6 +112,18 @@ int bl_random_coordinates(int n, double *xy);
 int bl_greedy_coordinates(int n, const int *rowptr, const int *colids, double *xy);
 int bl_write_coordinates(const char *input, const char *outputdir, const char *tag,
                          const double *xy, int n, char *path_out, int path_cap);
+/* The neighbours the reference's sorted-CSR cursor matches (kindex,
+ * sample/algorithms.cpp:746,758-762), host only: per row the longest
+ * strictly ascending prefix; an empty row i with a non-empty row after it
+ * matches colids[rowptr[i]], that row's first entry (the cursor starts there
+ * and the reference applies attraction to it); empty rows with no non-empty
+ * row after them match nothing.
+ * matched_rowptr receives n+1 offsets; matched_colids (may be NULL for a
+ * counting call) at least matched_rowptr[n] ids, which is at most
+ * rowptr[n] + (number of empty rows).  These are the lists every minibatch
+ * method attracts over; bl_minibatch_iteration_noalloc takes them as input. */
+int bl_cursor_neighbours(int n, const int *rowptr, const int *colids, int *matched_rowptr,
+                         int *matched_colids);
 
 /* ---- layout methods: out[0] = energy of the last iteration, out[1] = seconds
  * (wall time including the init, like omp_get_wtime() in the reference).
@@ -338,9 +351,12 @@ int bl_learned_layout(bl_ctx *ctx, const float *params, const double *scale_mode
  * 768 KiB device array inside the library, which limits batch to 256 and the
  * launch to 160 blocks (larger requests return BL_ERR_TOO_LARGE).
  * Device pointers, all caller-owned, on the current device:
- *   d_rowptr[n+1], d_colids   neighbour lists the minibatch cursor matches
- *                             (the CSR rows themselves when each row is sorted
- *                             ascending without duplicates)
+ *   d_rowptr[n+1], d_colids   neighbour lists the minibatch cursor matches,
+ *                             as bl_cursor_neighbours builds them on the host
+ *                             (the CSR rows themselves only when every row is
+ *                             sorted ascending without duplicates AND no row
+ *                             but the last is empty: an empty row matches the
+ *                             next row's first neighbour)
  *   d_xy[2n] float32           coordinates, updated in place
  *   d_force[2n], d_vertex_energy[n]  outputs: forces and |f|^2 per vertex
  * stream: cudaStream_t (NULL = default stream); the call returns after the

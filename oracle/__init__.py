@@ -47,6 +47,29 @@ def build(quiet: bool = True) -> None:
             raise RuntimeError("oracle build failed:\n" + out.decode())
 
 
+def reference_dir() -> str | None:
+    """Where the reference's sources are: $BL_REFERENCE_DIR, else a checkout
+    named `reference` beside this repository; None when neither holds
+    sample/algorithms.cpp."""
+    cands = [os.environ.get("BL_REFERENCE_DIR", ""),
+             os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for c in cands:
+        if c and os.path.isfile(os.path.join(c, "sample", "algorithms.cpp")):
+            return c
+    return None
+
+
+def build_reference(ref: str | None = None, quiet: bool = True) -> bool:
+    """Compile the reference from its own sources into oracle/_ref/ with
+    oracle/build_ref.sh (test infrastructure).  False when no sources."""
+    ref = ref or reference_dir()
+    if not ref:
+        return False
+    subprocess.run([os.path.join(HERE, "build_ref.sh"), ref], check=True,
+                   stdout=subprocess.DEVNULL if quiet else None)
+    return True
+
+
 _libs: dict[bool, C.CDLL] = {}
 
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C")

@@ -10,9 +10,13 @@
 #   oracle/_ref/ref_driver          oracle/ref_driver.cpp + sample/algorithms.cpp,
 #                                   strict flags: full-precision golden vectors
 #
-# usage: oracle/build_ref.sh [REFERENCE_DIR]   (default /root/reference)
+# usage: oracle/build_ref.sh REFERENCE_DIR   (or BL_REFERENCE_DIR in the environment)
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${BL_REFERENCE_DIR:-}}"
+if [ -z "$REF" ]; then
+  echo "usage: $0 REFERENCE_DIR (or set BL_REFERENCE_DIR)" >&2
+  exit 2
+fi
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/sample/algorithms.cpp" ]; then

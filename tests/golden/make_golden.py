@@ -1,6 +1,7 @@
 """Regenerate the golden fixtures in this directory from the reference itself.
 
-Needs the reference sources (default /root/reference); builds them with
+Needs the reference sources (REFERENCE_DIR, else $BL_REFERENCE_DIR or a
+`reference` checkout beside this repository); builds them with
 oracle/build_ref.sh into oracle/_ref/ and runs oracle/_ref/ref_driver, which
 calls the reference's own public routines and prints full-precision results.
 
@@ -129,7 +130,10 @@ def graphs():
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    import oracle
+    ref = sys.argv[1] if len(sys.argv) > 1 else oracle.reference_dir()
+    if not ref:
+        sys.exit("reference sources not found: pass REFERENCE_DIR or set BL_REFERENCE_DIR")
     subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh"), ref], check=True)
     drv = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
     stock = os.path.join(ROOT, "oracle", "_ref", "BatchLayout")

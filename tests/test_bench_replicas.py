@@ -74,6 +74,12 @@ def test_reference_arm_line_on_the_grid_workload():
     assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
     assert line["value"] > 0 and line["higher_is_better"] is True
     assert line["config"]["workload"].startswith("grid64")
+    # the same config object as the GPU arm's line (bench.workload_config)
+    from batchlayoutcode_gb300 import graphs as G
+    g, _ = G.cached_workload("grid64")
+    args = type("A", (), {"workload": "grid64"})()
+    assert line["config"] == bench.workload_config(args, bench.WORKLOADS["grid64"], g)
+    assert set(line["config"]) == {"workload", "vertices", "edges", "step", "l2"}
     cb = line["cpu_baseline"]
     assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == line["value"]
     assert line["e2e"] == {"value": line["value"], "unit": bench.UNIT, "h2d_bytes_per_step": 0,

@@ -264,6 +264,30 @@ def test_reader_binary_cache(L, tmp_path):
     assert not i4["cached"] and rp4.tolist() == [0, 1, 1, 2]
 
 
+def test_reader_binary_cache_same_name_size_and_mtime(L, tmp_path):
+    """Two different files with the same base name, size and modification
+    time (a copy kept with cp -p, an archive extracted twice) share a cache
+    directory: each read returns its own file's CSR."""
+    cache = tmp_path / "cache"
+    cache.mkdir()
+    a, b = tmp_path / "a", tmp_path / "b"
+    a.mkdir()
+    b.mkdir()
+    fa, fb = a / "g.mtx", b / "g.mtx"
+    fa.write_text("%%MatrixMarket matrix coordinate pattern general\n3 3 2\n1 2\n3 1\n")
+    fb.write_text("%%MatrixMarket matrix coordinate pattern general\n3 3 2\n2 1\n1 3\n")
+    st = os.stat(fa)
+    os.utime(fb, ns=(st.st_atime_ns, st.st_mtime_ns))
+    assert os.path.getsize(fa) == os.path.getsize(fb)
+    want = {str(fa): L.read_matrix_market(str(fa))[:2], str(fb): L.read_matrix_market(str(fb))[:2]}
+    assert want[str(fa)][1].tolist() != want[str(fb)][1].tolist()
+    for path in (fa, fb, fa, fa, fb, fb):
+        rp, ci, _ = L.read_matrix_market(str(path), str(cache))
+        assert rp.tolist() == want[str(path)][0].tolist() and ci.tolist() == want[str(path)][1].tolist()
+    rp, ci, info = L.read_matrix_market(str(fb), str(cache))
+    assert info["cached"]  # the cache now holds fb and serves it
+
+
 @pytest.mark.parametrize("damage", ["truncated", "rows", "huge_nnz", "colid", "rowptr", "magic"])
 def test_reader_binary_cache_damaged(L, tmp_path, damage):
     """A cache file whose stamp still matches the source but whose contents
@@ -280,7 +304,10 @@ def test_reader_binary_cache_damaged(L, tmp_path, damage):
     L.read_matrix_market(str(src), str(cache))
     f = cache / "g.mtx.blcsr"
     b = bytearray(f.read_bytes())
-    hdr = 48  # magic, source size, source mtime, rows, cols, nnz, symmetric, pad
+    # magic, source size, source mtime, rows, cols, nnz, symmetric, pad, device,
+    # inode, path length, pad, then the canonical path padded to 8 bytes
+    plen = struct.unpack_from("<i", b, 64)[0]
+    hdr = 72 + (plen + 7) // 8 * 8
     rows = struct.unpack_from("<i", b, 24)[0]
     if damage == "truncated":
         b = b[:-4]
@@ -300,6 +327,56 @@ def test_reader_binary_cache_damaged(L, tmp_path, damage):
     assert np.array_equal(rp, rp0) and np.array_equal(ci, ci0)
     rp, ci, info = L.read_matrix_market(str(src), str(cache))  # rewritten
     assert info["cached"] and np.array_equal(rp, rp0) and np.array_equal(ci, ci0)
+
+
+def _cursor_matches(rp, ci):
+    """The reference's kindex scan (sample/algorithms.cpp:746,758-762) written
+    out: for each target i the cursor starts at rowptr[i]; a source j equal to
+    colids[k] is a match (attraction) and the cursor advances while it is
+    before the row's last entry."""
+    n, nnz = len(rp) - 1, int(rp[-1])
+    out = []
+    for i in range(n):
+        k, m = int(rp[i]), []
+        for j in range(n):
+            if k < nnz and j == ci[k]:
+                m.append(j)
+                if k < rp[i + 1] - 1:
+                    k += 1
+        out.append(m)
+    return out
+
+
+def test_cursor_neighbours_match_the_reference_scan(L):
+    """bl_cursor_neighbours (host only) on rows that are sorted, unsorted,
+    repeated, empty in the middle and empty at the end."""
+    rng = np.random.default_rng(7)
+    for trial in range(40):
+        n = int(rng.integers(2, 40))
+        rows = []
+        for i in range(n):
+            kind = rng.integers(0, 5)
+            if kind == 0:
+                rows.append([])
+            else:
+                r = list(rng.integers(0, n, size=int(rng.integers(1, 6))))
+                if kind <= 2:
+                    r = sorted(r)
+                rows.append(r)
+        if trial % 4 == 0:
+            rows[-1] = []
+        rp = np.zeros(n + 1, np.int32)
+        rp[1:] = np.cumsum([len(r) for r in rows])
+        ci = np.array([c for r in rows for c in r] or [0], np.int32)[:rp[-1]]
+        if rp[-1] == 0:
+            continue
+        mrp, mci = L.cursor_neighbours(rp, ci)
+        want = _cursor_matches(rp, ci)
+        got = [list(mci[mrp[i]:mrp[i + 1]]) for i in range(n)]
+        assert got == want, (trial, rows)
+        assert mrp[-1] <= rp[-1] + sum(1 for r in rows if not r)
+    with pytest.raises(L.BatchLayoutError):
+        L.cursor_neighbours(np.array([0, 1], np.int32), np.array([5], np.int32))
 
 
 def test_writer_parallel_slices(L, tmp_path):
