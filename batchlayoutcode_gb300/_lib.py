@@ -29,7 +29,7 @@ EXPORTS = (
     "bl_learned_features", "bl_learned_train", "bl_learned_init", "bl_learned_layout",
     "bl_learned_load_model", "bl_approx_force_directed", "bl_cache_blocking_minibatch_sd",
     "bl_greedy_iteration", "bl_greedy_walks", "bl_read_matrix_market_cached", "bl_bfs_init",
-    "bl_cursor_neighbours",
+    "bl_cursor_neighbours", "bl_wait_selftest",
 )
 
 _lib = None
@@ -113,6 +113,7 @@ def load() -> C.CDLL:
         "bl_greedy_walks": (i32, [vp, C.POINTER(C.c_longlong), ip, ip, i64, C.POINTER(C.c_longlong)]),
         "bl_bfs_init": (i32, [vp]),
         "bl_cursor_neighbours": (i32, [i32, ip, ip, ip, ip]),
+        "bl_wait_selftest": (i32, [vp, i32, i32]),
         "bl_read_matrix_market_cached": (i32, [cp, cp, C.POINTER(C.c_longlong), dp, C.POINTER(ip), C.POINTER(ip),
                                                cp, i32]),
     }

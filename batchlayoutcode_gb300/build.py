@@ -24,7 +24,7 @@ LIB = os.path.join(OUT, "libbatchlayout_gb300.so")
 CLI = os.path.join(OUT, "batchlayout")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["minibatch.cu", "greedy.cu", "bfsinit.cu", "barnes_hut.cu", "batched.cu", "mpnn.cu", "features.cu", "learned.cu", "reduce.cu", "api.cu"]
+CU_SOURCES = ["minibatch.cu", "greedy.cu", "bfsinit.cu", "barnes_hut.cu", "batched.cu", "mpnn.cu", "features.cu", "learned.cu", "reduce.cu", "waits.cu", "api.cu"]
 CPP_SOURCES = ["host.cpp"]
 
 

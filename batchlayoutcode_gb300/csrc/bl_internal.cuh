@@ -31,6 +31,7 @@ struct DevStatus {
 
 // Timeouts for device waits (nanoseconds of %globaltimer).
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
+constexpr unsigned long long kMmaTimeoutNs = 1000000000ull;      // 1 s, tensor-core completion
 
 __device__ __forceinline__ unsigned long long dev_globaltimer() {
   unsigned long long t;

@@ -41,7 +41,6 @@ namespace bl {
 namespace {
 
 constexpr int kT = 128;                                    // vertices per tile = threads per block
-constexpr unsigned long long kMmaTimeoutNs = 1000000000ull;  // 1 s
 
 __device__ __forceinline__ void bf16x8_to_f32(uint4 q, float *f) {
   const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&q);

@@ -341,6 +341,18 @@ int bl_learned_init(bl_ctx *ctx, const float *params, const double *scale_model,
 int bl_learned_layout(bl_ctx *ctx, const float *params, const double *scale_model, int seed, int max_iterations,
                       int batch, double theta, double target_energy, double step0, double *out);
 
+/* ---- bounded device waits --------------------------------------------------- */
+
+/* No counterpart in the reference (which has no device waits).  Runs one of
+ * the bounded waits the layout kernels use, with its arrival made
+ * (complete = 1) or withheld (complete = 0): site 0 the grid barrier of the
+ * cooperative kernels (limit 2 s), site 1 the mbarrier wait for tensor-core
+ * completion (limit 1 s).  A withheld arrival lets the wait run to its limit;
+ * the kernel then records the site and returns, and the call returns
+ * BL_ERR_DEVICE_TIMEOUT with the reason in bl_last_error -- the path every
+ * layout call takes when a device wait runs out.  The context stays usable. */
+int bl_wait_selftest(bl_ctx *ctx, int site, int complete);
+
 /* ---- allocation-free variant ------------------------------------------------ */
 
 /* No counterpart in the reference.  One minibatch iteration (as

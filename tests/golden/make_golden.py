@@ -23,6 +23,13 @@ Outputs (committed):
     init_rand1               randInit coordinates with one thread
   ref_stdout_grid12*.txt     stdout of the stock BatchLayout binary (format test): algo 2
                              (1 iteration), algo 5 (6 iterations), algo 7 (1 iteration)
+  ref_grid64_cfg1.npz        the 64x64 triangulated grid, disc start (seed 1), algo 2,
+                             batch 256, 600 iterations: the reference's final energy
+                             from that start (`energy`), from five starts perturbed by
+                             1e-7 relative (`ensemble`, its chaotic spread), the start
+                             (`init_xy`) and the reference reader's CSR checksum
+
+    python tests/golden/make_golden.py [REFERENCE_DIR] [--cfg1]   (--cfg1: only that file)
 """
 from __future__ import annotations
 
@@ -129,14 +136,44 @@ def graphs():
     return out
 
 
+def config1(drv):
+    """The 4,096-vertex grid workload run by the reference for 600 iterations
+    of algo 2 at batch 256, from the start and from five perturbed starts."""
+    g, xy = G.workload("grid64")
+    xy = np.asarray(xy, np.float64)
+    rng = np.random.default_rng(11)
+    energies = []
+    with tempfile.TemporaryDirectory() as td:
+        mtx = os.path.join(td, "grid64.mtx")
+        G.write_mtx(g, mtx)
+        lines = run([drv, "csr", mtx]).splitlines()
+        rows, nnz = int(lines[0].split()[1]), int(lines[0].split()[3])
+        vals = np.array([int(v) for v in lines[1:]], np.int64)
+        assert np.array_equal(vals[: rows + 1], g.rowptr) and np.array_equal(vals[rows + 1: rows + 1 + nnz], g.colids)
+        for k in range(6):
+            start = xy if k == 0 else xy * (1.0 + 1e-7 * rng.standard_normal(xy.shape))
+            initf = os.path.join(td, f"start{k}.initf")
+            G.write_initf(start, initf)
+            lines = run([drv, "layout", mtx, initf, "2", "600", "256", "1.2", "1.0", "0.01", td + "/"]).splitlines()
+            energies.append(float(lines[0].split()[1]))
+    np.savez_compressed(os.path.join(HERE, "ref_grid64_cfg1.npz"), init_xy=xy, energy=np.array(energies[0]),
+                        ensemble=np.array(energies), iterations=np.array(600), batch=np.array(256),
+                        csr_sum=np.array([g.n, g.nnz, int(np.sum(g.colids, dtype=np.int64))]))
+    print("grid64 cfg1", energies)
+
+
 def main():
     import oracle
-    ref = sys.argv[1] if len(sys.argv) > 1 else oracle.reference_dir()
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref = args[0] if args else oracle.reference_dir()
     if not ref:
         sys.exit("reference sources not found: pass REFERENCE_DIR or set BL_REFERENCE_DIR")
     subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh"), ref], check=True)
     drv = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
     stock = os.path.join(ROOT, "oracle", "_ref", "BatchLayout")
+    if "--cfg1" in sys.argv:
+        config1(drv)
+        return
     for name, g, xy in graphs():
         mtx = os.path.join(HERE, f"{name}.mtx")
         initf = os.path.join(HERE, f"{name}.initf")

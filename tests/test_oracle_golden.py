@@ -84,3 +84,19 @@ def test_greedy_walks_follow_the_reference_rules(gold):
             for v in w:
                 reach |= set(ci[rp[v]:rp[v + 1]].tolist())
             assert reach - excl <= set(w.tolist())
+
+
+def test_grid64_600_iterations_energy_bit_exact():
+    """The 4,096-vertex triangulated grid workload (algo 2, batch 256, 600
+    iterations from the seeded disc start): the oracle's final energy equals
+    the reference's own (strict build) bit for bit, and the reader's CSR
+    checksum matches the generator's graph."""
+    import os
+    from batchlayoutcode_gb300 import graphs as G
+    from conftest import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "ref_grid64_cfg1.npz"))
+    g, xy = G.workload("grid64")
+    assert np.array_equal(np.asarray(xy, np.float64), z["init_xy"])
+    assert z["csr_sum"].tolist() == [g.n, g.nnz, int(np.sum(g.colids, dtype=np.int64))]
+    _, e, _ = oracle.layout(2, g.rowptr, g.colids, z["init_xy"], int(z["iterations"]), int(z["batch"]))
+    assert e == float(z["energy"])
