@@ -77,6 +77,7 @@ int bl_check_status(bl_ctx *ctx) {
                      : st.code == DEV_TIMEOUT_TREE        ? "tree build wait timed out"
                      : st.code == DEV_FORCE_RANGE         ? "force beyond the fixed-point range (coincident vertices?)"
                      : st.code == DEV_TIMEOUT_MMA         ? "tensor-core MMA completion wait timed out"
+                     : st.code == DEV_TIMEOUT_SWEEP       ? "level sweep wait for a moved neighbour timed out"
                                                           : "device error";
   cudaMemset(ctx->s.status, 0, sizeof(DevStatus));
   return bl_fail(ctx, BL_ERR_DEVICE_TIMEOUT,
@@ -719,7 +720,7 @@ int bl_morton_order(bl_ctx *ctx, double *frame, unsigned long long *keys, int *p
   const int n = ctx->g.n;
   if (n < 2) return bl_fail(ctx, BL_ERR_ARG, "need at least two vertices");
   if (int rc = bl::ensure_bh_scratch(ctx)) return rc;
-  if (int rc = bl::bh_build(ctx, ctx->pos)) return rc;
+  if (int rc = bl::bh_build(ctx, ctx->pos, 1.2)) return rc;  // (theta enters only the records)
   BL_CUDA(ctx, cudaMemcpyAsync(frame, ctx->s.frame, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   BL_CUDA(ctx, cudaMemcpyAsync(keys, ctx->s.keys, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream));
   BL_CUDA(ctx, cudaMemcpyAsync(perm, ctx->s.perm, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
@@ -743,7 +744,7 @@ int bl_bh_repulsion(bl_ctx *ctx, double theta, double *out, long long *stats) tr
   BL_CUDA(ctx, cudaSetDevice(ctx->device));
   const int n = ctx->g.n;
   if (int rc = bl::ensure_bh_scratch(ctx)) return rc;
-  if (int rc = bl::bh_build(ctx, ctx->pos)) return rc;
+  if (int rc = bl::bh_build(ctx, ctx->pos, theta)) return rc;
   if (int rc = bl::bh_traverse(ctx, theta, true, 0)) return rc;
   std::vector<float2> rep(n);
   unsigned long long st[2] = {0, 0};

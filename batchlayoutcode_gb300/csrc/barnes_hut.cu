@@ -824,6 +824,7 @@ __global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
 
 struct LayoutArgs {
   int n;
+  double inv_theta2;  // 1 / theta^2, folded into the records' z
   DevStatus *st;
   const float2 *spos;
   const int2 *range;
@@ -851,7 +852,7 @@ __global__ void layout_kernel(LayoutArgs L, TreeArgs t) {
       return;
     }
     const float2 p = L.spos[i];
-    L.nodes[idx] = make_float4(p.x, p.y, 0.0f, __int_as_float(idx + 1));
+    L.nodes[idx] = make_float4(p.x, p.y, kLeafZ, __int_as_float(idx + 1));
     L.nodes_c64[idx] = make_double2(f2d_int(p.x), f2d_int(p.y));
     L.nodes_lvl[idx] = 255;
   }
@@ -869,7 +870,7 @@ __global__ void layout_kernel(LayoutArgs L, TreeArgs t) {
     }
     const double D = ldexp(maxmin, -lvl);
     const double2 c = L.qcen[i];
-    L.nodes[idx] = make_float4(d2f_int(c.x), d2f_int(c.y), d2f_int(D * D), __int_as_float(skip));
+    L.nodes[idx] = make_float4(d2f_int(c.x), d2f_int(c.y), bh_record_z(D, L.inv_theta2), __int_as_float(skip));
     L.nodes_c64[idx] = c;
     L.nodes_lvl[idx] = (unsigned char)lvl;
   }
@@ -885,7 +886,6 @@ struct TraverseArgs {
   const float2 *spos;
   const int *perm;
   float2 *rep;
-  float theta2;
   double theta;
   unsigned long long *stats;  // [visits, fp64 decisions] or null
   // attraction of neighbours that have not moved yet in this iteration
@@ -916,7 +916,7 @@ __global__ void __launch_bounds__(kTravThreads) traverse_kernel(TraverseArgs a) 
     total = 0;
   }
   unsigned int visits = 0, exact = 0;
-  const float2 rep = bh_repulsion<true, kStats>(a.nodes, a.nodes_c64, a.nodes_lvl, a.frame[2], a.theta2, a.theta,
+  const float2 rep = bh_repulsion<true, kStats>(a.nodes, a.nodes_c64, a.nodes_lvl, a.frame[2], a.theta,
                                                 total, q, visits, exact);
   const int v = a.perm[k];
   a.rep[v] = rep;
@@ -941,7 +941,7 @@ struct SweepArgs {
   int levels;
   const float4 *f0;      // attraction of unmoved neighbours minus repulsion (float-float)
   const float2 *pold;
-  float2 *pnew;
+  float2 *pnew;          // every entry kUnmoved before the launch
   double2 *force;
   double *e;
   int write_out;
@@ -952,14 +952,55 @@ struct SweepArgs {
 
 constexpr int kSweepThreads = 1024;
 
+// A new position not yet written: both coordinates NaN, all bits set
+// (no layout coordinate is NaN).  pnew is filled with it before the sweep.
+constexpr unsigned long long kUnmoved = 0xffffffffffffffffull;
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const float2 *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_relaxed_u64(float2 *p, float2 v) {
+  const unsigned long long b =
+      (unsigned long long)__float_as_uint(v.x) | ((unsigned long long)__float_as_uint(v.y) << 32);
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(b) : "memory");
+}
+
+__device__ __forceinline__ float2 unpack_pos(unsigned long long b) {
+  return make_float2(__uint_as_float((unsigned int)b), __uint_as_float((unsigned int)(b >> 32)));
+}
+
+// The new position of neighbour c, which an earlier dependency level writes:
+// the 8-byte word is the position and its own ready flag (a single-copy
+// atomic 64-bit access), so one load both tests and reads it.  The wait is
+// bounded; false when it ran out or another thread recorded an error.
+__device__ __forceinline__ bool wait_moved(const SweepArgs &a, int c, unsigned long long &b) {
+  if (b != kUnmoved) return true;
+  const unsigned long long t0 = dev_globaltimer();
+  for (unsigned int polls = 1;; polls++) {
+    b = ld_relaxed_u64(&a.pnew[c]);
+    if (b != kUnmoved) return true;
+    if ((polls & 63u) == 0u) {
+      if (ld_volatile_u32(&a.st->code) != 0u) return false;
+      if (dev_globaltimer() - t0 > kBarrierTimeoutNs) {
+        dev_record_error(a.st, DEV_TIMEOUT_SWEEP);
+        return false;
+      }
+    }
+  }
+}
+
 // A vertex's data that does not change during the sweep: its slot in the
-// level order, id, iteration-start position, f0 and earlier-batch neighbour
-// range.
+// level order, id, iteration-start position, f0, earlier-batch neighbour
+// range and the first four of those neighbours (most vertices have no more).
 struct SweepVertex {
   int t, i;
   float2 pi;
   float4 f;
   int e0, e1;
+  int c[4];
 };
 
 __device__ __forceinline__ void sweep_load(const SweepArgs &a, int t, SweepVertex &v) {
@@ -969,73 +1010,98 @@ __device__ __forceinline__ void sweep_load(const SweepArgs &a, int t, SweepVerte
   v.f = a.f0[v.i];
   v.e0 = a.early_off[t];
   v.e1 = a.early_off[t + 1];
+#pragma unroll
+  for (int q = 0; q < 4; q++) v.c[q] = (v.e0 + q < v.e1) ? a.early_col[v.e0 + q] : 0;
 }
 
 // Adds the attraction of the neighbours that moved earlier in this iteration
-// (earlier batches, their new positions) to f0, then the unit-step update
-// (algorithms.cpp:1056-1066).  FP32 terms, float-float sum, FP32 unit vector.
-__device__ __forceinline__ void sweep_vertex(const SweepArgs &a, const SweepVertex &v) {
+// (earlier batches, their new positions, each waited for) to f0, then the
+// unit-step update (algorithms.cpp:1056-1066).  FP32 terms, float-float sum,
+// FP32 unit vector.  False when a wait gave up.
+__device__ __forceinline__ bool sweep_vertex(const SweepArgs &a, const SweepVertex &v) {
   float hx = v.f.x, hy = v.f.y, lx = v.f.z, ly = v.f.w;
-  int e = v.e0;
-  // the gathers of up to four moved neighbours are issued together; the
-  // terms are added in neighbour order
-  for (; e + 4 <= v.e1; e += 4) {
-    const int c0 = a.early_col[e], c1 = a.early_col[e + 1], c2 = a.early_col[e + 2], c3 = a.early_col[e + 3];
-    const float2 q0 = __ldcg(&a.pnew[c0]), q1 = __ldcg(&a.pnew[c1]), q2 = __ldcg(&a.pnew[c2]),
-                 q3 = __ldcg(&a.pnew[c3]);
-    bh_attract(q0, v.pi, a.W, hx, lx, hy, ly);
-    bh_attract(q1, v.pi, a.W, hx, lx, hy, ly);
-    bh_attract(q2, v.pi, a.W, hx, lx, hy, ly);
-    bh_attract(q3, v.pi, a.W, hx, lx, hy, ly);
+  const int m = min(v.e1 - v.e0, 4);
+  // the loads of the first (up to) four moved neighbours are issued
+  // together; the terms are added in neighbour order
+  unsigned long long b[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) b[q] = (q < m) ? ld_relaxed_u64(&a.pnew[v.c[q]]) : 0ull;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    if (q < m) {
+      if (!wait_moved(a, v.c[q], b[q])) return false;
+      bh_attract(unpack_pos(b[q]), v.pi, a.W, hx, lx, hy, ly);
+    }
   }
-  if (e + 2 <= v.e1) {
-    const int c0 = a.early_col[e], c1 = a.early_col[e + 1];
-    const float2 q0 = __ldcg(&a.pnew[c0]), q1 = __ldcg(&a.pnew[c1]);
-    bh_attract(q0, v.pi, a.W, hx, lx, hy, ly);
-    bh_attract(q1, v.pi, a.W, hx, lx, hy, ly);
-    e += 2;
+  // more than four (rare): one at a time
+  for (int e = v.e0 + 4; e < v.e1; e++) {
+    const int c = a.early_col[e];
+    unsigned long long bb = ld_relaxed_u64(&a.pnew[c]);
+    if (!wait_moved(a, c, bb)) return false;
+    bh_attract(unpack_pos(bb), v.pi, a.W, hx, lx, hy, ly);
   }
-  if (e < v.e1) bh_attract(__ldcg(&a.pnew[a.early_col[e]]), v.pi, a.W, hx, lx, hy, ly);
   const float2 np = bh_step(v.pi, hx, lx, hy, ly, a.step);
-  a.pnew[v.i] = np;
   if (a.write_out) {
     const double fx = (double)hx + (double)lx, fy = (double)hy + (double)ly;
     a.force[v.i] = make_double2(fx, fy);
     a.e[v.i] = fx * fx + fy * fy;
   }
+  st_relaxed_u64(&a.pnew[v.i], np);  // publishes the position: later levels wait for this word
+  return true;
 }
 
-// One cooperative launch for all dependency levels of an iteration; a
-// bounded grid barrier separates the levels.  Between a thread's arrival at
-// the barrier and its wait, it loads its first vertex of the next level
-// (nothing of it changes during the sweep), so a level after the barrier
-// costs the gathers of the moved neighbours only.
+// All dependency levels of an iteration in one launch, without barriers: a
+// vertex waits only for the new positions of its own earlier-batch
+// neighbours (bounded waits on their position words).  The slots of each
+// level are cut into 32-slot groups, numbered across the levels in level
+// order, and group G goes to warp G mod W (W warps in the grid, numbered so
+// that consecutive groups land on different SMs): every warp gets about the
+// same number of groups, and takes them in level order.  A warp finishes a
+// level (__syncwarp) before it starts the next, so a slot waits only on slots
+// of lower levels held by other warps or by this warp's finished groups; with
+// every block resident (a cooperative launch) the warp holding the lowest
+// unfinished slot can always proceed, so the sweep cannot deadlock.  A thread
+// loads its next slot's vertex data before it waits on the current slot's
+// neighbours.
 __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs a) {
-  if (!block_status_ok(a.st)) return;  // every block sees the same value: no barrier is left waiting
-  unsigned int epoch = 0;
-  const int gsz = gridDim.x * blockDim.x;
-  // slot group k (32 consecutive slots of a level) goes to warp k / gridDim.x
-  // of block k % gridDim.x: a small level spreads over every SM instead of
-  // filling the first blocks
-  const int t0 = (((int)threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x) * 32 + ((int)threadIdx.x & 31);
-  SweepVertex first;
-  first.t = -1;
-  if (a.levels > 0 && a.level_off[0] + t0 < a.level_off[1]) sweep_load(a, a.level_off[0] + t0, first);
-  for (int l = 0; l < a.levels; l++) {
-    const int lo = a.level_off[l], hi = a.level_off[l + 1];
-    if (first.t >= 0) sweep_vertex(a, first);
-    for (int t = lo + t0 + gsz; t < hi; t += gsz) {
-      SweepVertex v;
-      sweep_load(a, t, v);
-      sweep_vertex(a, v);
+  if (!block_status_ok(a.st)) return;
+  const int W = gridDim.x * (blockDim.x >> 5);
+  const int lane = threadIdx.x & 31;
+  const int w = ((int)threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x;
+  // (lv, j): the warp's current group j of level lv; gb: groups of the levels below lv
+  int lv = 0, j = 0;
+  long long gb = 0;
+  auto first_group = [&](int l, long long base) { return (int)((((long long)w - base) % W + W) % W); };
+  auto settle = [&](int &l, int &jj, long long &base) {
+    while (l < a.levels) {
+      const int lo = a.level_off[l], hi = a.level_off[l + 1];
+      if (lo + 32 * jj < hi) return;
+      base += (hi - lo + 31) / 32;
+      l++;
+      jj = first_group(l, base);
     }
-    if (l + 1 < a.levels) {
-      grid_arrive(a.st, epoch);
-      first.t = -1;
-      const int nlo = a.level_off[l + 1];
-      if (nlo + t0 < a.level_off[l + 2]) sweep_load(a, nlo + t0, first);
-      if (!grid_wait(a.st, epoch)) return;
-    }
+  };
+  j = first_group(0, 0);
+  settle(lv, j, gb);
+  auto slot = [&](int l, int jj) { return a.level_off[l] + 32 * jj + lane; };
+  SweepVertex cur{};
+  bool has = lv < a.levels && slot(lv, j) < a.level_off[lv + 1];
+  if (has) sweep_load(a, slot(lv, j), cur);
+  bool ok = true;
+  while (lv < a.levels) {
+    int nlv = lv, nj = j + W;
+    long long ngb = gb;
+    settle(nlv, nj, ngb);
+    SweepVertex nxt{};
+    const bool nhas = nlv < a.levels && slot(nlv, nj) < a.level_off[nlv + 1];
+    if (nhas) sweep_load(a, slot(nlv, nj), nxt);
+    if (has && ok) ok = sweep_vertex(a, cur);
+    if (nlv != lv) __syncwarp();  // the warp's level is done before its next level starts
+    lv = nlv;
+    j = nj;
+    gb = ngb;
+    cur = nxt;
+    has = nhas;
   }
 }
 
@@ -1097,7 +1163,7 @@ int ensure_bh_scratch(bl_ctx *ctx) {
 // Steps 1-4 for the positions `pos`; leaves the pre-order records in
 // ctx->s.nodes (total = n + number of quad nodes, read back by callers that
 // need it via startbase[n]).
-int bh_build(bl_ctx *ctx, const float2 *pos) {
+int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
   const int n = ctx->g.n;
   Scratch &s = ctx->s;
   cudaStream_t st = ctx->stream;
@@ -1177,6 +1243,7 @@ int bh_build(bl_ctx *ctx, const float2 *pos) {
   if (int rc = scan_exclusive_int(ctx, s.startcnt, s.startbase, n + 1)) return rc;
   LayoutArgs L;
   L.n = n;
+  L.inv_theta2 = 1.0 / (theta * theta);
   L.spos = s.spos;
   L.range = s.brange;
   L.dlt = s.bdelta;
@@ -1215,7 +1282,6 @@ int bh_traverse(bl_ctx *ctx, double theta, bool want_stats, int batch) {
   a.perm = s.perm;
   a.rep = s.rep;
   a.theta = theta;
-  a.theta2 = (float)(theta * theta);
   a.stats = want_stats ? s.stats : nullptr;
   a.st = s.status;
   a.f0 = batch > 0 ? s.f0 : nullptr;
@@ -1240,7 +1306,7 @@ int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_en
   const LevelSchedule *ls = level_schedule(ctx, batch);
   if (!ls) return -2;
   float2 *pold = ctx->pos, *pnew = ctx->s.pos_alt;
-  if (int rc = bh_build(ctx, pold)) return rc;
+  if (int rc = bh_build(ctx, pold, theta)) return rc;
   if (int rc = bh_traverse(ctx, theta, false, batch)) return rc;
   SweepArgs a;
   a.order = ls->order;
@@ -1261,7 +1327,8 @@ int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_en
   BL_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sweep_kernel, kSweepThreads, 0));
   if (occ < 1) return bl_fail(ctx, -5, "sweep kernel cannot be resident");
   const int sweep_grid = ctx->num_sms * std::min(occ, 2);
-  BL_CUDA(ctx, cudaMemsetAsync(&ctx->s.status->barrier, 0, sizeof(unsigned int), ctx->stream));
+  // every new position starts as "not written": the sweep's waits read it
+  BL_CUDA(ctx, cudaMemsetAsync(pnew, 0xff, (size_t)ctx->g.n * sizeof(float2), ctx->stream));
   void *args[] = {&a};
   bl_time_begin(ctx, "sweep_kernel");
   BL_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)sweep_kernel, dim3(sweep_grid), dim3(kSweepThreads),
@@ -1464,7 +1531,7 @@ int bh_canonical_tree(bl_ctx *ctx, int cap, int *lo, int *hi, int *depth, int *n
   if (n < 2) return 0;
   if (int rc = ensure_bh_scratch(ctx)) return rc;
   if (n < 2) return 0;
-  if (int rc = bh_build(ctx, ctx->pos)) return rc;
+  if (int rc = bh_build(ctx, ctx->pos, 1.2)) return rc;  // (theta enters only the records)
   // copy the binary tree back and emit quad nodes in pre-order (host walk)
   std::vector<int2> child(n - 1), range(n - 1);
   std::vector<int> dlt(n - 1), parent(2 * n - 1);

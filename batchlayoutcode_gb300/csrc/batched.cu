@@ -48,8 +48,8 @@ struct BatchedGraph {
 
 struct BatchedArgs {
   int num_graphs, iterations, batch;
-  float W, theta2;
-  double theta;
+  float W;
+  double theta, inv_theta2;  // inv_theta2 = 1 / theta^2, folded into the records
   const BatchedGraph *graphs;
   const int *order;            // queue order (largest graph first)
   unsigned int *queue;         // next queue slot
@@ -249,7 +249,7 @@ __device__ __forceinline__ void write_leaf(const BatchedArgs &a, float4 *nodes, 
     return;
   }
   const float2 p = spos[k];
-  nodes[idx] = make_float4(p.x, p.y, 0.0f, __int_as_float(idx + 1));
+  nodes[idx] = make_float4(p.x, p.y, kLeafZ, __int_as_float(idx + 1));
   c64[idx] = make_double2((double)p.x, (double)p.y);
   nlvl[idx] = 255;
 }
@@ -541,7 +541,7 @@ __device__ void layout_bh(const BatchedArgs &a, int g, BhShared &S, double *red)
         }
         const double D = ldexp(maxmin, -lv);
         const double2 c = bcen[q];
-        nodes[I] = make_float4((float)c.x, (float)c.y, (float)(D * D), __int_as_float(I + sz));
+        nodes[I] = make_float4(d2f_int(c.x), d2f_int(c.y), bh_record_z(D, a.inv_theta2), __int_as_float(I + sz));
         c64[I] = c;
         nlvl[I] = (unsigned char)lv;
         int run = I + 1;
@@ -575,7 +575,7 @@ __device__ void layout_bh(const BatchedArgs &a, int g, BhShared &S, double *red)
       }
       unsigned int visits = 0, exact = 0;
       for (int k = tid; k < n; k += kBThreads) {
-        const float2 rep = bh_repulsion<false>(nodes, c64, nlvl, maxmin, a.theta2, a.theta, total, spos[k], visits,
+        const float2 rep = bh_repulsion<false>(nodes, c64, nlvl, maxmin, a.theta, total, spos[k], visits,
                                                exact);
         const int v = vin[k];
         f0[v] = bh_unmoved_attraction(v, rep, rp, ci, pos, a.batch, a.W);
@@ -925,7 +925,7 @@ int bl_batched_run(bl_ctx *ctx, int iterations, int batch, double theta, double 
   a.batch = batch;
   a.W = (float)weight;
   a.theta = theta;
-  a.theta2 = (float)(theta * theta);
+  a.inv_theta2 = 1.0 / (theta * theta);
   if (int rc = batched_shape(ctx, *B, batch)) return rc;
   if (int rc = batched_autotune(ctx, *B)) return rc;
   if (B->graph_dirty || B->key_iterations != iterations || B->key_batch != batch || B->key_theta != theta ||

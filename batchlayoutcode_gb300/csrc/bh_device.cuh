@@ -165,30 +165,43 @@ static __device__ __noinline__ bool open_test_fp64(const double2 *c64, const uns
   return __ddiv_rn(D, dist) < theta;
 }
 
-// Error-bound constants of bh_walk_step for a query q.  The bound of the FP32
-// comparison |theta^2 d^2 - D^2|, with a wide safety factor, is 2^-20
-// (theta^2 d^2 + D^2) for the centroid, theta^2 and D^2 roundings and the
-// products, plus theta^2 2^-21 s (|qx| + |qy| + |x| + |y|) <= theta^2 2^-21 s
-// (2 (|qx| + |qy|) + s), s = |dx| + |dy|, for the rounding of the coordinates
-// and of their differences.
-__device__ __forceinline__ float bh_tol_a(float theta2) { return theta2 * 4.7683716e-07f * 1.001f; }
-__device__ __forceinline__ float bh_tol_q(float ta, float2 q) { return ta * 2.f * (fabsf(q.x) + fabsf(q.y)); }
+// Pre-order record {x, y, z, skip} of the walk: a quad node's FP32 centroid,
+// z = D^2 / theta^2 rounded to FP32 (D its diameter, BarnesHut.h:128,157, the
+// threshold of the opening test folded in), and the record after its
+// subtree; a leaf point's coordinates, z = -inf (always added) and the next
+// record.
+constexpr float kLeafZ = -__builtin_huge_valf();
+
+__device__ __forceinline__ float bh_record_z(double D, double inv_theta2) {
+  return d2f_int(__dmul_rn(__dmul_rn(D, D), inv_theta2));
+}
+
+// Error bound of the FP32 opening test m = d^2 - z > 0 (the reference's
+// D / dist < theta is dist^2 > D^2 / theta^2): 2^-18 d^2 for the roundings of
+// the centroid, of z and of the products (a wide margin over a few ulp; when
+// z > 3 d^2 the margin |m| > 2 d^2 is never in doubt), plus
+// 2^-21 s (2 (|qx| + |qy|) + s), s = |dx| + |dy|, for the rounding of the
+// coordinates and of their differences (with 0.2 % to spare).
+constexpr float kTolRel = 3.8146973e-06f;        // 2^-18
+constexpr float kTolA = 4.7683716e-07f * 1.002f;  // 2^-21
+__device__ __forceinline__ float bh_tol_q(float2 q) { return kTolA * 2.f * (fabsf(q.x) + fabsf(q.y)); }
 
 // One record of the walk: the opening test on record i, the accepted
-// record's unit vector added to (fx, fy), and the next record.
+// record's unit vector added to (fx, fy), and the next record.  The FP32 test
+// decides unless its margin is within the error bound; then the FP64 test
+// (the reference's own arithmetic) decides.
 template <bool kRO, bool kStats>
 __device__ __forceinline__ void bh_walk_step(const float4 *nodes, const double2 *c64, const unsigned char *lvl,
-                                             double maxmin, float theta2, double theta, float ta, float tq, float2 q,
-                                             int &i, float &fx, float &fy, unsigned int &visits,
-                                             unsigned int &exact) {
+                                             double maxmin, double theta, float tq, float2 q, int &i, float &fx,
+                                             float &fy, unsigned int &visits, unsigned int &exact) {
   const float4 nd = ldx<kRO>(&nodes[i]);
   const float dx = nd.x - q.x, dy = nd.y - q.y;
   const float d2 = fmaf(dx, dx, fmaf(dy, dy, kTinyD2));
-  const float lhs = theta2 * d2;
-  bool accept = nd.z < lhs;
+  const float m = d2 - nd.z;  // +inf for a leaf
+  bool accept = m > 0.f;
   const float sd = fabsf(dx) + fabsf(dy);
-  const float tol = fmaf(sd, fmaf(ta, sd, tq), 9.5367432e-07f * (lhs + nd.z));
-  if (fabsf(lhs - nd.z) <= tol && nd.z > 0.f) {
+  const float tol = fmaf(sd, fmaf(kTolA, sd, tq), kTolRel * d2);
+  if (fabsf(m) <= tol) {
     accept = open_test_fp64<kRO>(c64, lvl, maxmin, theta, i, q.x, q.y);
     if (kStats) exact++;
   }
@@ -201,23 +214,21 @@ __device__ __forceinline__ void bh_walk_step(const float4 *nodes, const double2 
   i = accept ? max(__float_as_int(nd.w), i + 1) : i + 1;
 }
 
-// Stackless walk of the pre-order records {x, y, D^2, skip} (record 0 is the
-// root, its skip link is the number of records): repulsion on q
-// (BarnesHut.h:69-86).  The opening test D/dist < theta is evaluated in FP32
-// and re-evaluated in FP64 when the FP32 margin is within its error bound, so
-// every decision equals the reference's FP64 decision.  A leaf at q itself
-// adds nothing (its vector is zero).  The step to the next record is
-// max(skip, i + 1) on acceptance, so the walk ends after at most `total`
-// records whatever the records hold (the layout checks every skip link).
-// kStats counts record visits and FP64 decisions.
+// Stackless walk of the pre-order records (record 0 is the root, its skip
+// link is the number of records): repulsion on q (BarnesHut.h:69-86).  Every
+// decision equals the reference's FP64 decision (see bh_walk_step).  A leaf
+// at q itself adds nothing (its vector is zero).  The step to the next
+// record is max(skip, i + 1) on acceptance, so the walk ends after at most
+// `total` records whatever the records hold (the layout checks every skip
+// link).  kStats counts record visits and FP64 decisions.
 template <bool kRO, bool kStats = false>
 __device__ __forceinline__ float2 bh_repulsion(const float4 *nodes, const double2 *c64, const unsigned char *lvl,
-                                               double maxmin, float theta2, double theta, int total, float2 q,
+                                               double maxmin, double theta, int total, float2 q,
                                                unsigned int &visits, unsigned int &exact) {
-  const float ta = bh_tol_a(theta2), tq = bh_tol_q(ta, q);
+  const float tq = bh_tol_q(q);
   float fx = 0.f, fy = 0.f;
   int i = 0;
-  while (i < total) bh_walk_step<kRO, kStats>(nodes, c64, lvl, maxmin, theta2, theta, ta, tq, q, i, fx, fy, visits, exact);
+  while (i < total) bh_walk_step<kRO, kStats>(nodes, c64, lvl, maxmin, theta, tq, q, i, fx, fy, visits, exact);
   return make_float2(fx, fy);
 }
 

@@ -20,6 +20,7 @@ enum : unsigned int {
   DEV_BAD_INDEX = 3,
   DEV_FORCE_RANGE = 4,
   DEV_TIMEOUT_MMA = 5,
+  DEV_TIMEOUT_SWEEP = 6,
 };
 
 struct DevStatus {
@@ -292,7 +293,7 @@ int greedy_walks_build(bl_ctx *ctx);
 int greedy_walk_run(bl_ctx *ctx, int batch, int iterations, double step0, double decay, bool want_energy,
                     double *energy_out);
 int ensure_bh_scratch(bl_ctx *ctx);
-int bh_build(bl_ctx *ctx, const float2 *pos);
+int bh_build(bl_ctx *ctx, const float2 *pos, double theta);  // theta: folded into the walk records
 int bh_traverse(bl_ctx *ctx, double theta, bool want_stats, int batch);
 int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_energy,
                  double *energy_out);

@@ -194,7 +194,7 @@ int learned_init(bl_ctx *ctx, const float *params, const double *scale_model, in
     // the attraction A grows with the square of the scale, so
     // sum_v |k^2 A_v - R_v|^2 is least at k^2 = sum A.R / sum |A|^2.
     if (!rc) rc = ensure_bh_scratch(ctx);
-    if (!rc) rc = bh_build(ctx, ctx->pos);
+    if (!rc) rc = bh_build(ctx, ctx->pos, 1.2);
     if (!rc) rc = bh_traverse(ctx, 1.2, false, 0);
     if (!rc) {
       double *d_p2 = nullptr;

@@ -708,6 +708,9 @@ def main():
                     help="skip the all-pairs minibatch figure on the 100k Chung-Lu graph in the default line")
     ap.add_argument("--stages", action="store_true",
                     help="Barnes-Hut workloads: print the live time of every stage of one iteration and exit")
+    ap.add_argument("--traverse-probe", action="store_true",
+                    help="Barnes-Hut workloads: after --warmup iterations print the traversal's record visits, "
+                         "then run one iteration (its traverse_kernel launch walks the same tree) and exit")
     ap.add_argument("--io", action="store_true",
                     help="host only: time the MatrixMarket reader, the binary CSR cache and the output writer "
                          "on the 1M-vertex graph, print one JSON line and exit")
@@ -760,6 +763,18 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
     if args.stages and w["algo"] == 4:
         print(json.dumps(stage_times(a, w, flush, args.steps, args.warmup)))
+        return
+    if args.traverse_probe and w["algo"] == 4:
+        # `warmup` iterations, the record visits of the repulsion walk at that
+        # state (the counting instance), then one iteration whose traversal
+        # launch (the timed instance) walks the same tree: an ncu capture of
+        # that launch gives the warp instructions for exactly these visits
+        a.set_graph_mode(False)  # direct launches: traverse_kernel<false> launch number warmup + 1 is the one
+        a.run_resident(4, args.warmup, w["batch"], w["theta"], 1.0, want_energy=False)
+        _, (visits, exact) = a.bh_repulsion(w["theta"])
+        a.barnes_hut_iteration(w["batch"], w["theta"], 0.999 ** args.warmup)
+        print(json.dumps({"traverse_probe": {"workload": args.workload, "iterations_before": args.warmup,
+                                             "record_visits": visits, "fp64_retests": exact}}))
         return
     algo, batch, theta = w["algo"], w["batch"], w["theta"]
     ips = w.get("iters_per_step", 1)

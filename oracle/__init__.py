@@ -84,7 +84,7 @@ def lib(fast: bool = False) -> C.CDLL:
     L = C.CDLL(os.path.join(BUILD, "liboracle_fast.so" if fast else "liboracle.so"))
     L.orc_morton_sort.argtypes = [C.c_int, _f64p, _f64p, _u64p, _i32p]
     L.orc_bh_tree.argtypes = [C.c_int, _f64p, C.c_int, _i32p, _i32p, _i32p, _i32p, _f64p]
-    L.orc_bh_repulsion.argtypes = [C.c_int, _f64p, C.c_int, _f64p, C.c_double, _f64p, C.c_int]
+    L.orc_bh_repulsion.argtypes = [C.c_int, _f64p, C.c_int, _f64p, C.c_double, _f64p, C.c_int, C.c_void_p]
     L.orc_layout.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, C.c_int, C.c_int, C.c_double,
                              C.c_double, C.c_double, C.c_double, C.c_int, C.c_void_p, _f64p]
     L.orc_smu_iteration.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, C.c_int, C.c_double,
@@ -132,12 +132,16 @@ def bh_tree(xy: np.ndarray) -> dict:
     return dict(lo=lo[:m], hi=hi[:m], depth=dep[:m], nchild=nc[:m], centroid=cxy[: 2 * m].reshape(m, 2))
 
 
-def bh_repulsion(tree_xy: np.ndarray, queries: np.ndarray, theta: float, nthreads=None) -> np.ndarray:
+def bh_repulsion(tree_xy: np.ndarray, queries: np.ndarray, theta: float, nthreads=None, visits: bool = False):
+    """Barnes-Hut repulsion of every query; with visits=True also the number
+    of tree records (nodes tested, leaf points reached) each walk reads."""
     t = np.ascontiguousarray(tree_xy, dtype=np.float64)
     q = np.ascontiguousarray(queries, dtype=np.float64)
     out = np.zeros_like(q)
-    lib().orc_bh_repulsion(t.shape[0], t.ravel(), q.shape[0], q.ravel(), theta, out.ravel(), _threads(nthreads))
-    return out
+    vis = np.zeros(q.shape[0], np.int64) if visits else None
+    lib().orc_bh_repulsion(t.shape[0], t.ravel(), q.shape[0], q.ravel(), theta, out.ravel(), _threads(nthreads),
+                           vis.ctypes.data if visits else None)
+    return (out, vis) if visits else out
 
 
 def layout(algo: int, rowptr, colids, xy, iterations: int, batch: int = 256, theta: float = 1.2,

@@ -292,9 +292,24 @@ void build_tree(Tree &t, int n, const P2 *p, Frame &frame, std::vector<int> &per
   build_node(t, 0, n, 0, frame.maxmin / 1.0);  // gridLength(1), BarnesHut.h:128
 }
 
+// `visits` (optional) counts the records a stackless pre-order walk of the
+// canonical tree (no single-child chain nodes) reads for the same decisions:
+// the leaf points reached and the nodes tested, where a chain of
+// single-child nodes counts once (its head is tested; the canonical node at
+// its foot has the same centroid and a smaller diameter, so it is accepted
+// whenever the head is, and is tested in the head's place otherwise).
+static int present_children(const Tree &t, const Node &nd) {
+  if (nd.depth >= 32) return nd.hi - nd.lo;
+  int nc = 0;
+  for (int k = 0; k < 4; k++) nc += (nd.child[k] >= 0) || (nd.leaf[k] >= 0);
+  (void)t;
+  return nc;
+}
+
 void bh_force(const Tree &t, int node, const P2 &v, double theta, double &fx,
-              double &fy) {
+              double &fy, long long *visits = nullptr, bool counted = true) {
   const Node &nd = t.nodes[node];
+  if (visits && counted) ++*visits;
   const double dx = nd.cx - v.x, dy = nd.cy - v.y;
   const double distance = std::sqrt(dx * dx + dy * dy);
   if (nd.diameter / distance < theta) {
@@ -305,8 +320,9 @@ void bh_force(const Tree &t, int node, const P2 &v, double theta, double &fx,
   }
   for (int k = 0; k < 4; k++) {
     if (nd.child[k] >= 0) {
-      bh_force(t, nd.child[k], v, theta, fx, fy);
+      bh_force(t, nd.child[k], v, theta, fx, fy, visits, visits && present_children(t, nd) >= 2);
     } else if (nd.leaf[k] >= 0) {
+      if (visits) ++*visits;
       const P2 &q = t.pts[nd.leaf[k]];
       const double ex = q.x - v.x, ey = q.y - v.y;
       const double den = std::sqrt(ex * ex + ey * ey);
@@ -319,6 +335,7 @@ void bh_force(const Tree &t, int node, const P2 &v, double theta, double &fx,
   }
   if (nd.depth >= 32) {
     for (int p = nd.lo; p < nd.hi; p++) {
+      if (visits) ++*visits;
       const P2 &q = t.pts[p];
       const double ex = q.x - v.x, ey = q.y - v.y;
       const double den = std::sqrt(ex * ex + ey * ey);
@@ -644,7 +661,7 @@ int orc_bh_tree(int n, const double *xy, int cap, int *lo, int *hi, int *depth,
 // Barnes-Hut repulsion R(v) = sum of unit vectors (BarnesHut.h:69-86) for
 // each query, from the tree built over tree_xy.  The layout step subtracts it.
 int orc_bh_repulsion(int n, const double *tree_xy, int nq, const double *q_xy,
-                     double theta, double *out, int nthreads) {
+                     double theta, double *out, int nthreads, long long *visits_out) {
   const P2 *p = reinterpret_cast<const P2 *>(tree_xy);
   Tree t;
   Frame fr;
@@ -654,9 +671,11 @@ int orc_bh_repulsion(int n, const double *tree_xy, int nq, const double *q_xy,
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads)
   for (int i = 0; i < nq; i++) {
     double fx = 0.0, fy = 0.0;
-    bh_force(t, 0, q[i], theta, fx, fy);
+    long long vis = 0;
+    bh_force(t, 0, q[i], theta, fx, fy, visits_out ? &vis : nullptr);
     out[2 * i] = fx;
     out[2 * i + 1] = fy;
+    if (visits_out) visits_out[i] = vis;
   }
   return 0;
 }

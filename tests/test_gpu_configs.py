@@ -18,14 +18,18 @@ ensemble's spread, as stated per test:
 * 1M-vertex random geometric graph, algo 4, batch 256, 20 iterations: within
   0.5 % of the oracle ensemble's mean (or three of its standard deviations);
 * the 2,048-graph batched mix, 300 iterations (algo 2 below 5,000 vertices,
-  algo 4 above): every 64th graph by size against a four-member oracle
-  ensemble per graph.  On these small graphs the reference's own runs from
-  starts 1e-7 apart end 1 % to 35 % apart (relative standard deviations of
-  0.4 % to 17 %, measured), so a single graph is held to the larger of 0.5 %
-  and six standard deviations (its own or the pooled relative spread of its
-  method, whichever is larger), and the whole sample to the geometric mean of
-  the 32 ratios GPU / ensemble mean within three standard errors of 1: a bias
-  of the pipeline would move every ratio the same way.
+  algo 4 above).  On these small graphs the energy of one iteration is a
+  heavy-tailed quantity: the reference's own runs from starts 1e-7 apart end
+  1 % to 35 % apart, and along one run the energy of consecutive iterations
+  swings by a factor of two (a 1,038-vertex Chung-Lu graph: 1.07e6 to 2.28e6
+  over its last 50 iterations, measured).  So the sample (every 64th graph by
+  size) is checked in two ways: along the device's own trajectory every
+  checked iteration (1, 150, 300) of six graphs of both methods equals the
+  reference's step from the device's states (energy within 2e-5, the
+  single-graph force tolerance); and over all 32 graphs the median ratio of
+  the device's final energy to a four-member oracle ensemble's mean is 1
+  within three standard errors (a bias of the pipeline would move every
+  ratio the same way).
 """
 import os
 
@@ -98,7 +102,19 @@ def test_rgg1m_algo4_20_iterations_energy(B):
     assert abs(e - mean) <= max(5e-3 * mean, 3.0 * sd), (e, ens)
 
 
-def test_batched2048_sample_against_oracle_ensembles(B):
+def _batched_run(B, graphs, algo, xys, ks, iters):
+    """Coordinates and last energies of graphs `ks` after `iters` iterations,
+    laid out together in one batched launch (the start itself for 0)."""
+    if iters == 0:
+        return [np.asarray(xys[k], np.float64) for k in ks], None
+    with B.BatchedLayout([graphs[k] for k in ks], np.asarray(algo)[ks], [xys[k] for k in ks]) as bl:
+        bl.set_parts([2, 2, 2])  # the same source split in every run, so the runs share one trajectory
+        bl.run(iters, 256, 1.2)
+        xs, es = bl.result()
+    return xs, es
+
+
+def test_batched2048_sample_against_the_reference(B):
     import sys
     from conftest import ROOT
     sys.path.insert(0, ROOT)
@@ -109,21 +125,29 @@ def test_batched2048_sample_against_oracle_ensembles(B):
         bl.run(iters, 256, 1.2)
         _, energies = bl.result()
     pick, _ = bench.batched_sample(graphs, algo, iters)
+    # 1. every checked iteration of six sampled graphs (four minibatch, two
+    #    Barnes-Hut) is the reference's step from the device's own states
+    chosen = [pick[i] for i in (0, 11, 16, 22, 24, 31)]
+    assert sorted({int(algo[k]) for k in chosen}) == [2, 4]
+    for it in (1, 150, 300):
+        before, _ = _batched_run(B, graphs, algo, xys, chosen, it - 1)
+        after, es = _batched_run(B, graphs, algo, xys, chosen, it)
+        for k, x0, x1, e in zip(chosen, before, after, es):
+            rp, ci = graphs[k]
+            _, te = oracle.forces_on_trajectory(int(algo[k]), rp, ci, x0, x1, 256)
+            assert abs(e - te) <= 2 * FORCE_TOL * te, (k, it, e, te)
+    # 2. the final energies of all 32 sampled graphs against the oracle's
     rng = np.random.default_rng(5)
-    rows = []
+    logr, rel = [], []
     for k in pick:
         rp, ci = graphs[k]
         xy = np.asarray(xys[k], np.float64)
         ens = np.array([oracle.layout(int(algo[k]), rp, ci,
                                       xy if r == 0 else xy * (1 + 1e-7 * rng.standard_normal(xy.shape)),
                                       iters, 256, 1.2, fast=True)[1] for r in range(4)])
-        rows.append((k, int(algo[k]), float(energies[k]), float(ens.mean()), float(ens.std(ddof=1) / ens.mean())))
-    pooled = {m: float(np.sqrt(np.mean([r[4] ** 2 for r in rows if r[1] == m]))) for m in {r[1] for r in rows}}
-    for k, m, e, mean, rel in rows:
-        bound = max(5e-3, 6.0 * max(rel, pooled[m]))
-        assert abs(e / mean - 1.0) <= bound, (k, len(graphs[k][0]) - 1, m, e, mean, rel, pooled[m])
-    ratios = np.log([e / mean for _, _, e, mean, _ in rows])
-    # the GPU run is one more member of each ensemble: its log ratio to the
-    # mean of four has variance 1.25 rel^2
-    se = float(np.sqrt(np.mean([r[4] ** 2 for r in rows]) * 1.25 / len(rows)))
-    assert abs(float(ratios.mean())) <= max(5e-3, 3.0 * se), (ratios.mean(), se, rows)
+        logr.append(float(np.log(energies[k] / ens.mean())))
+        rel.append(float(ens.std(ddof=1) / ens.mean()))
+    # the median of 32 ratios: standard error 1.2533 sigma / sqrt(32), the
+    # device run being one more member of each ensemble (variance 1.25 rel^2)
+    se = 1.2533 * float(np.sqrt(1.25 * np.mean(np.square(rel)) / len(logr)))
+    assert abs(float(np.median(logr))) <= max(5e-3, 3.0 * se), (np.median(logr), se, logr)

@@ -158,11 +158,17 @@ def test_quadtree_bit_exact(B, gold):
 
 @pytest.mark.parametrize("theta", [1.2, 0.5])
 def test_bh_repulsion(B, gold, theta):
+    """Repulsion within 1e-5 of the reference's, and every opening decision
+    the reference's: the walks read exactly as many records as the oracle's
+    recursion tests nodes and reaches leaf points."""
     _, z = gold
     with make(B, z) as a:
         rep, (visits, exact) = a.bh_repulsion(theta)
     assert visits > 0
     assert rel_l2(rep, z[f"bh_rep_t{theta}"]) <= FORCE_TOL
+    orep, ovis = oracle.bh_repulsion(z["init_xy"], z["init_xy"], theta, visits=True)
+    assert np.array_equal(orep, z[f"bh_rep_t{theta}"])
+    assert visits == int(ovis.sum())
 
 
 @pytest.mark.parametrize("batch", [32, 256])
@@ -354,6 +360,21 @@ def test_rgg1m_bh_iteration_forces(B, rgg1m):
     tf, te = oracle.forces_on_trajectory(4, g.rowptr, g.colids, xy, xe, 256)
     assert rel_l2(f, tf) <= FORCE_TOL
     assert abs(e - te) / te <= 2 * FORCE_TOL
+
+
+@pytest.mark.parametrize("theta", [1.2, 0.5])
+def test_rgg1m_traversal_decisions_exact(B, rgg1m, theta):
+    """On the 1M-vertex graph the walks read exactly the records the oracle's
+    recursion reaches (every FP32 opening test that could differ from the FP64
+    one is redone in FP64), and the repulsion is within 1e-5."""
+    g, xy = rgg1m
+    xy = np.asarray(xy, np.float64)
+    with B.Algorithms(g.rowptr, g.colids) as a:
+        a.nCoordinates = xy
+        rep, (visits, exact) = a.bh_repulsion(theta)
+    orep, ovis = oracle.bh_repulsion(xy, xy, theta, visits=True)
+    assert visits == int(ovis.sum())
+    assert rel_l2(rep, orep) <= FORCE_TOL
 
 
 def test_chunglu100k_minibatch_iteration_forces(B):

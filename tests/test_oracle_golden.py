@@ -100,3 +100,57 @@ def test_grid64_600_iterations_energy_bit_exact():
     assert z["csr_sum"].tolist() == [g.n, g.nnz, int(np.sum(g.colids, dtype=np.int64))]
     _, e, _ = oracle.layout(2, g.rowptr, g.colids, z["init_xy"], int(z["iterations"]), int(z["batch"]))
     assert e == float(z["energy"])
+
+
+def _canonical_walk_visits(xy, theta):
+    """Records read by a pre-order walk of the canonical tree (oracle.bh_tree:
+    nodes with two or more children, and the leaf points) that opens a node
+    when D / dist >= theta, D = MAXMIN 2^-depth (BarnesHut.h:71-72): what the
+    device's stackless walk reads for the same decisions."""
+    import math
+    import sys
+    sys.setrecursionlimit(10000)
+    frame, _, perm = oracle.morton_sort(xy)
+    t = oracle.bh_tree(xy)
+    lo, hi, dep, cen = t["lo"], t["hi"], t["depth"], t["centroid"]
+    kids = [[] for _ in range(len(lo))]
+    stack = []
+    for k in range(len(lo)):
+        while stack and not (lo[k] >= lo[stack[-1]] and hi[k] <= hi[stack[-1]]):
+            stack.pop()
+        if stack:
+            kids[stack[-1]].append(k)
+        stack.append(k)
+    total = 0
+    for q in xy:
+        count = [0]
+
+        def visit(k):
+            count[0] += 1
+            dx, dy = cen[k][0] - q[0], cen[k][1] - q[1]
+            dist = math.sqrt(dx * dx + dy * dy)
+            if dist > 0 and math.ldexp(frame[2], -int(dep[k])) / dist < theta:
+                return
+            p, c = lo[k], 0
+            while p < hi[k]:
+                if c < len(kids[k]) and lo[kids[k][c]] == p:
+                    visit(kids[k][c])
+                    p = hi[kids[k][c]]
+                    c += 1
+                else:
+                    count[0] += 1
+                    p += 1
+        visit(0)
+        total += count[0]
+    return total
+
+
+@pytest.mark.parametrize("theta", [1.2, 0.5])
+def test_bh_visit_count_is_the_canonical_walk(gold, theta):
+    """The oracle's per-query visit counts (its recursion over the reference
+    quadtree, a single-child chain counted once) add up to the records a walk
+    of the canonical tree reads: the figure the device's walk is held to."""
+    _, z = gold
+    xy = z["init_xy"]
+    _, vis = oracle.bh_repulsion(xy, xy, theta, visits=True)
+    assert int(vis.sum()) == _canonical_walk_visits(xy, theta)
