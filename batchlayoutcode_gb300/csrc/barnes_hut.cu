@@ -980,6 +980,7 @@ __device__ __forceinline__ bool wait_moved(const SweepArgs &a, int c, unsigned l
   if (b != kUnmoved) return true;
   const unsigned long long t0 = dev_globaltimer();
   for (unsigned int polls = 1;; polls++) {
+    __nanosleep(100);  // fewer polls queued at L2 while the writer works
     b = ld_relaxed_u64(&a.pnew[c]);
     if (b != kUnmoved) return true;
     if ((polls & 63u) == 0u) {
