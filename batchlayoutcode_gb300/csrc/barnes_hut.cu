@@ -113,42 +113,56 @@ __global__ void __launch_bounds__(256) rs_rowscan_kernel(unsigned int *hist, int
   if (tid == 0) row_total[blockIdx.x] = carry;
 }
 
+// Exclusive scan of one value per thread over a 256-thread block (ws: 8
+// words of shared scratch); every thread calls it.
+__device__ __forceinline__ unsigned int rs_block_scan256(unsigned int v, unsigned int *ws) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  unsigned int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[warp] = x;
+  __syncthreads();
+  unsigned int wpre = 0;
+#pragma unroll
+  for (int k = 0; k < kRsWarps; k++)
+    if (k < warp) wpre += ws[k];
+  __syncthreads();
+  return wpre + x - v;
+}
+
+// The tile's keys are ranked (stably: warp order, then lane order within a
+// warp's 32-key rows), placed in shared memory grouped by digit, and written
+// out from there: consecutive threads write consecutive keys of a digit's
+// run, so each run of the tile reaches L2 as whole sectors rather than as one
+// partial sector per key.
 __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
     const u64 *__restrict__ kin, const int *__restrict__ vin, u64 *__restrict__ kout, int *__restrict__ vout,
     int n, int shift, int ntiles, const unsigned int *__restrict__ hist, const unsigned int *__restrict__ row_total) {
-  __shared__ unsigned int s_cnt[kRsWarps][256];  // per-warp counts, then per-warp offsets
-  __shared__ unsigned int s_base[256];
+  __shared__ unsigned int s_cnt[kRsWarps][256];  // per-warp counts, then per-warp offsets within the digit
+  __shared__ unsigned int s_base[256];            // global position of the tile's first key of each digit
+  __shared__ unsigned int s_loc[256];             // position of the tile's first key of each digit in the tile
   __shared__ unsigned int s_ws[kRsWarps];
+  __shared__ u64 s_key[kRsTile];
+  __shared__ int s_val[kRsTile];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 #pragma unroll
   for (int w = 0; w < kRsWarps; w++) s_cnt[w][tid] = 0;
-  {
-    // digit offset = exclusive scan of the 256 row totals (every block does it)
-    const unsigned int v = row_total[tid];
-    unsigned int x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) s_ws[warp] = x;
-    __syncthreads();
-    unsigned int wpre = 0;
-#pragma unroll
-    for (int k = 0; k < kRsWarps; k++)
-      if (k < warp) wpre += s_ws[k];
-    s_base[tid] = wpre + x - v + hist[(size_t)tid * ntiles + blockIdx.x];
-  }
-  __syncthreads();
+  // digit offset = exclusive scan of the 256 row totals (every block does it)
+  s_base[tid] = rs_block_scan256(row_total[tid], s_ws) + hist[(size_t)tid * ntiles + blockIdx.x];
   const int wbase = blockIdx.x * kRsTile + warp * (kRsItems * 32);
   const unsigned int lt = (1u << lane) - 1u;
   u64 key[kRsItems];
+  int val[kRsItems];
   unsigned int rd[kRsItems];  // rank within the warp's keys (low 16 bits) | digit << 16, digit 256 = none
 #pragma unroll
   for (int r = 0; r < kRsItems; r++) {
     const int idx = wbase + r * 32 + lane;
     const bool valid = idx < n;
     key[r] = valid ? kin[idx] : 0ull;
+    val[r] = valid ? vin[idx] : 0;
     const unsigned int d = valid ? ((unsigned int)(key[r] >> shift) & 255u) : 256u;
     const unsigned int peers = __match_any_sync(0xffffffffu, d);
     const unsigned int leader = __ffs(peers) - 1;
@@ -167,16 +181,26 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
     s_cnt[w][tid] = run;
     run += c;
   }
+  s_loc[tid] = rs_block_scan256(run, s_ws);  // its barriers also publish s_cnt
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < kRsItems; r++) {
     const unsigned int d = rd[r] >> 16;
     if (d < 256u) {
-      const unsigned int p = s_base[d] + s_cnt[warp][d] + (rd[r] & 0xffffu);
-      if (p < (unsigned int)n) {
-        kout[p] = key[r];
-        vout[p] = vin[wbase + r * 32 + lane];
-      }
+      const unsigned int p = s_loc[d] + s_cnt[warp][d] + (rd[r] & 0xffffu);
+      s_key[p] = key[r];
+      s_val[p] = val[r];
+    }
+  }
+  __syncthreads();
+  const int cnt = min(kRsTile, n - (int)blockIdx.x * kRsTile);
+  for (int p = tid; p < cnt; p += kRsThreads) {
+    const u64 k = s_key[p];
+    const unsigned int d = (unsigned int)(k >> shift) & 255u;
+    const unsigned int g = s_base[d] + ((unsigned int)p - s_loc[d]);
+    if (g < (unsigned int)n) {
+      kout[g] = k;
+      vout[g] = s_val[p];
     }
   }
 }
@@ -852,9 +876,8 @@ __global__ void layout_kernel(LayoutArgs L, TreeArgs t) {
       return;
     }
     const float2 p = L.spos[i];
+    // a leaf's z = -inf is never in doubt: no FP64 centroid or level needed
     L.nodes[idx] = make_float4(p.x, p.y, kLeafZ, __int_as_float(idx + 1));
-    L.nodes_c64[idx] = make_double2(f2d_int(p.x), f2d_int(p.y));
-    L.nodes_lvl[idx] = 255;
   }
   if (i < L.n - 1 && !is_sub(t, i)) {  // quad node = binary internal node i
     const int2 rg = L.range[i];
