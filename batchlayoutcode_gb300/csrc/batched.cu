@@ -329,9 +329,15 @@ __device__ void layout_bh(const BatchedArgs &a, int g, BhShared &S, double *red)
       }
     }
     __syncthreads();
-    // 3. stable LSD radix sort, 8-bit digits; a pass whose digit is the same
-    //    for every key is skipped
-    for (int pass = 0; pass < 8; pass++) {
+    // 3. stable LSD radix sort of (key, vertex), 8-bit digits: the four
+    //    passes on the high 32 bits, then every run of equal high halves (two
+    //    points in one cell of a 65,536 x 65,536 grid over the frame: rare)
+    //    sorted on its own by (key, vertex) -- the order the whole-device path
+    //    produces.  A run longer than 32 keys sends the block through the
+    //    four low passes and the high ones again instead (the order of equal
+    //    keys, vertex order, is kept by every pass).  A pass whose digit is
+    //    the same for every key is skipped.
+    auto lsd_pass = [&](int pass) {
       const int shift = 8 * pass;
       if (tid < 256) S.cnt[tid] = 0;
       if (tid == 0) S.trivial = 0;
@@ -359,7 +365,7 @@ __device__ void layout_bh(const BatchedArgs &a, int g, BhShared &S, double *red)
       __syncthreads();
       const int trivial = S.trivial;
       __syncthreads();  // S.trivial is rewritten at the start of the next pass
-      if (trivial) continue;
+      if (trivial) return;
       for (int tile0 = 0; tile0 < n; tile0 += kSortTile) {
         for (int d = lane; d < 256; d += 32) S.wcnt[warp][d] = 0;
         __syncwarp();
@@ -415,7 +421,38 @@ __device__ void layout_bh(const BatchedArgs &a, int g, BhShared &S, double *red)
       int *tv = vin;
       vin = vout;
       vout = tv;
+    };
+    for (int pass = 4; pass < 8; pass++) lsd_pass(pass);
+    if (tid == 0) S.trivial = 0;  // reused: a run longer than 32 keys
+    __syncthreads();
+    for (int k = tid; k < n; k += kBThreads) {
+      const unsigned int h = (unsigned int)(kin[k] >> 32);
+      if (k > 0 && (unsigned int)(kin[k - 1] >> 32) == h) continue;       // not a run start
+      if (k + 1 >= n || (unsigned int)(kin[k + 1] >> 32) != h) continue;  // a run of one
+      int len = 2;
+      while (k + len < n && (unsigned int)(kin[k + len] >> 32) == h && len <= 32) len++;  // bounded
+      if (len > 32) {
+        S.trivial = 1;
+        continue;
+      }
+      for (int q = k + 1; q < k + len; q++) {  // insertion sort by (key, vertex)
+        const u64 kq = kin[q];
+        const int vq = vin[q];
+        int b = q - 1;
+        while (b >= k && (kin[b] > kq || (kin[b] == kq && vin[b] > vq))) {
+          kin[b + 1] = kin[b];
+          vin[b + 1] = vin[b];
+          b--;
+        }
+        kin[b + 1] = kq;
+        vin[b + 1] = vq;
+      }
     }
+    __syncthreads();
+    const int long_run = S.trivial;
+    __syncthreads();
+    if (long_run)
+      for (int pass = 0; pass < 8; pass++) lsd_pass(pass);
     // 4. positions in Morton order
     for (int k = tid; k < n; k += kBThreads) {
       int v = vin[k];

@@ -65,24 +65,30 @@ def load_model(path: str | None = None):
     return params, sm
 
 
-def training_graphs(count: int, lo: int, hi: int, seed: int = 1000):
-    """Seeded graphs of the benchmark mix with log-uniform sizes."""
+def _training_graph(k: int, n: int, seed: int):
+    kind = k % 3
+    if kind == 0:
+        r = max(2, int(round(math.sqrt(n))))
+        return G.grid_triangulated(r, max(2, int(round(n / r))))
+    if kind == 1:
+        return G.random_geometric(n, 6.0, seed=seed * 7919 + k)
+    g = G.chung_lu(n, 2.5, 8.0, seed=seed * 7919 + k)
+    g.values = None
+    return g
+
+
+def training_graphs(count: int, lo: int, hi: int, seed: int = 1000, workers: int = 1):
+    """Seeded graphs of the benchmark mix with log-uniform sizes (graph k is
+    the same whatever the number of worker processes)."""
     rng = np.random.default_rng(seed)
-    sizes = np.exp(rng.uniform(math.log(lo), math.log(hi), size=count))
-    out = []
-    for k, s in enumerate(sizes):
-        n = max(16, int(round(s)))
-        kind = k % 3
-        if kind == 0:
-            r = max(2, int(round(math.sqrt(n))))
-            g = G.grid_triangulated(r, max(2, int(round(n / r))))
-        elif kind == 1:
-            g = G.random_geometric(n, 6.0, seed=seed * 7919 + k)
-        else:
-            g = G.chung_lu(n, 2.5, 8.0, seed=seed * 7919 + k)
-            g.values = None
-        out.append(g)
-    return out
+    sizes = [max(16, int(round(s))) for s in np.exp(rng.uniform(math.log(lo), math.log(hi), size=count))]
+    if workers <= 1:
+        return [_training_graph(k, n, seed) for k, n in enumerate(sizes)]
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    # spawn: the workers start clean (no CUDA state is inherited)
+    with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_training_graph, range(count), sizes, [seed] * count, chunksize=4))
 
 
 def mds_start(g, edge_length: float = EDGE_LENGTH, seed: int = 1, device: int = 0) -> np.ndarray:
@@ -139,6 +145,8 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=2000)
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--seed", type=int, default=1000)
+    ap.add_argument("--workers", type=int, default=os.cpu_count() or 1,
+                    help="processes generating the training graphs")
     args = ap.parse_args(argv)
     if not args.train:
         ap.print_help()
@@ -146,7 +154,7 @@ def main(argv=None):
     from .build import build
     build()
     t0 = time.time()
-    gs = training_graphs(args.graphs, args.lo, args.hi, args.seed)
+    gs = training_graphs(args.graphs, args.lo, args.hi, args.seed, args.workers)
     t1 = time.time()
     lays = target_layouts(gs, args.iterations)
     t2 = time.time()

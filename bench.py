@@ -407,6 +407,28 @@ def time_to_energy(B, g, w, iterations: int = 600):
     # the plain run from the breadth-first greedy start built on the device
     with B.Algorithms(g.rowptr, g.colids, init=4) as a:
         e_bfs, bfs_s = a.BarnesHutApproximation(iterations, 0, w["batch"], w["theta"], 0)
+    # what the network itself buys: the lowest energy the same pipeline with a
+    # zero network (the pivot-MDS shape) reaches in its first 100 refinement
+    # iterations, then the iterations and seconds each start needs to reach it
+    floor_its = 100
+    with B.Algorithms(g.rowptr, g.colids, init=0) as a:
+        a.learnedInit(np.zeros_like(params), sm)
+        es, step = [], LR.STEP0
+        for _ in range(floor_its):
+            es.append(a.barnes_hut_iteration(w["batch"], w["theta"], step))
+            step *= 0.999
+    floor = min(es) * 1.005
+    with B.Algorithms(g.rowptr, g.colids, init=0) as a:
+        rf = a.learnedLayout(params, sm, floor_its, floor, w["batch"], w["theta"], LR.STEP0)
+    with B.Algorithms(g.rowptr, g.colids, init=0) as a:
+        rf0 = a.learnedLayout(np.zeros_like(params), sm, floor_its, floor, w["batch"], w["theta"], LR.STEP0)
+    network_gain = {
+        "target": f"lowest energy of the zero-network pipeline in its first {floor_its} refinement iterations x 1.005",
+        "target_energy": floor, "zero_network_best_iteration": int(np.argmin(es)) + 1,
+        "learned_iterations": rf["iterations"], "learned_s": rf["seconds"], "learned_fell_back": rf["fell_back"],
+        "mds_only_iterations": rf0["iterations"], "mds_only_s": rf0["seconds"], "mds_only_fell_back": rf0["fell_back"],
+        "speedup": rf0["seconds"] / rf["seconds"] if rf["seconds"] > 0 and not rf["fell_back"] else None,
+    }
     flops = 2.0 * g.n * (32 * 64 + 2 * 128 * 64)
     return {
         "plain_energy": e_plain, "plain_s": plain_s,
@@ -417,6 +439,7 @@ def time_to_energy(B, g, w, iterations: int = 600):
         "bfs_start_plain_s": bfs_s, "bfs_start_plain_energy": e_bfs,
         "mpnn_forward_ms": fwd_ms, "mpnn_forward_tflops": flops / (fwd_ms * 1e-3) / 1e12 if fwd_ms > 0 else None,
         "target": "plain run's final energy x 1.005",
+        "network_gain": network_gain,
         "note": "wall seconds through the C ABI, starts included (greedy DFS on the host; features, network "
                 "and scale on the device); refinement STEP from 0.3; model batchlayoutcode_gb300/weights/"
                 "mpnn_bh.blw (48 graphs of 1k-100k vertices); mds_only = the same pipeline with a zero network; "

@@ -1,8 +1,9 @@
 """The learned initializer end to end on the GPU: training lowers the loss,
 the shipped model's start reaches the plain run's final energy within a few
 Barnes-Hut iterations (the plain run needs all 600), the network beats the
-same pipeline without it (zero network output: the pivot-MDS shape), the
-plain run is the fallback, and the CLI accepts -learned."""
+same pipeline without it (zero network output: the pivot-MDS shape) both in
+its first iteration and in the iterations it needs to reach that pipeline's
+best energy, the plain run is the fallback, and the CLI accepts -learned."""
 import os
 import subprocess
 
@@ -54,6 +55,36 @@ def test_network_gains_over_mds_shape(B, rgg):
             a.learnedInit(p, sm)
             e[name] = a.barnes_hut_iteration(256, 1.2, LR.STEP0)
     assert e["learned"] < 0.95 * e["mds"], e
+
+
+@pytest.mark.parametrize("name", ["rgg1m", "grid300"])
+def test_network_reaches_the_zero_networks_best_energy_in_fewer_iterations(B, name):
+    """On held-out graphs -- the 1M-vertex benchmark graph and a 300 x 300
+    triangulated grid -- the lowest energy the pipeline without the network
+    (the pivot-MDS shape) reaches in its first 100 refinement iterations is
+    reached from the network's start in at most a quarter as many iterations
+    (measured: 1 against 42 and 1 against 56).  The energy, sum |f|^2 of an
+    iteration, is not monotone in the iterations (it settles at a level the
+    step size sets), so the target is the zero network's best, not its last.
+    On 100k-vertex random geometric graphs the gain depends on the graph (6
+    against 43 iterations on one seed, the target missed within 100 on
+    another) and on Chung-Lu graphs there is none."""
+    from batchlayoutcode_gb300 import graphs as G
+    from batchlayoutcode_gb300 import learned as LR
+    g = G.cached_workload("rgg1m")[0] if name == "rgg1m" else G.grid_triangulated(300, 300)
+    params, sm = LR.load_model()
+    with B.Algorithms(g.rowptr, g.colids, init=0) as a:
+        a.learnedInit(np.zeros_like(params), sm)
+        es, step = [], LR.STEP0
+        for _ in range(100):
+            es.append(a.barnes_hut_iteration(256, 1.2, step))
+            step *= 0.999
+    floor = min(es) * 1.005
+    zero_its = int(np.argmax(np.array(es) <= floor)) + 1
+    with B.Algorithms(g.rowptr, g.colids, init=0) as a:
+        r = a.learnedLayout(params, sm, 100, floor)
+    assert not r["fell_back"] and r["energy"] <= floor
+    assert 4 * r["iterations"] <= zero_its, (r["iterations"], zero_its, es)
 
 
 def test_fallback_is_the_plain_run(B):
