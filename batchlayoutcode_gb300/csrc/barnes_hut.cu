@@ -963,10 +963,9 @@ struct SweepArgs {
   const int *early_col;
   int levels;
   const float4 *f0;      // attraction of unmoved neighbours minus repulsion (float-float)
+  float4 *f0out;         // the same array: the final float-float force when write_out
   const float2 *pold;
   float2 *pnew;          // every entry kUnmoved before the launch
-  double2 *force;
-  double *e;
   int write_out;
   float W;
   float step;
@@ -1065,11 +1064,9 @@ __device__ __forceinline__ bool sweep_vertex(const SweepArgs &a, const SweepVert
     bh_attract(unpack_pos(bb), v.pi, a.W, hx, lx, hy, ly);
   }
   const float2 np = bh_step(v.pi, hx, lx, hy, ly, a.step);
-  if (a.write_out) {
-    const double fx = (double)hx + (double)lx, fy = (double)hy + (double)ly;
-    a.force[v.i] = make_double2(fx, fy);
-    a.e[v.i] = fx * fx + fy * fy;
-  }
+  // the force's float-float sums replace f0 (read above, not needed again);
+  // bh_forces_kernel turns them into the FP64 force and |f|^2 in full warps
+  if (a.write_out) a.f0out[v.i] = make_float4(hx, hy, lx, ly);
   st_relaxed_u64(&a.pnew[v.i], np);  // publishes the position: later levels wait for this word
   return true;
 }
@@ -1127,6 +1124,20 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs a) {
     cur = nxt;
     has = nhas;
   }
+}
+
+// The FP64 force f = hi + lo of each vertex (exact conversions, one addition
+// per component) and |f|^2, from the float-float sums the sweep left: the
+// values the reference's prevCoordinates and energy take, computed in full
+// warps by vertex id.
+__global__ void bh_forces_kernel(const float4 *__restrict__ ff, int n, double2 *__restrict__ force,
+                                 double *__restrict__ e) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 v = ff[i];
+  const double fx = __dadd_rn(f2d_int(v.x), f2d_int(v.z)), fy = __dadd_rn(f2d_int(v.y), f2d_int(v.w));
+  force[i] = make_double2(fx, fy);
+  e[i] = __fma_rn(fx, fx, __dmul_rn(fy, fy));
 }
 
 inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
@@ -1339,10 +1350,9 @@ int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_en
   a.early_col = ls->early_col;
   a.levels = ls->levels;
   a.f0 = ctx->s.f0;
+  a.f0out = ctx->s.f0;
   a.pold = pold;
   a.pnew = pnew;
-  a.force = ctx->force;
-  a.e = ctx->e;
   a.write_out = want_energy ? 1 : 0;
   a.W = (float)ctx->weight;
   a.step = (float)step;
@@ -1361,6 +1371,8 @@ int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_en
   ctx->launches++;
   std::swap(ctx->pos, ctx->s.pos_alt);
   if (want_energy) {
+    bh_forces_kernel<<<nblk(ctx->g.n, 256), 256, 0, ctx->stream>>>(ctx->s.f0, ctx->g.n, ctx->force, ctx->e);
+    ctx->launches++;
     if (int rc = energy_reduce(ctx, energy_out)) return rc;
     // without a destination (a captured iteration) the energy stays in
     // s.energy for the caller to read after the replay

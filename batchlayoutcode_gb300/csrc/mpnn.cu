@@ -41,6 +41,7 @@ namespace bl {
 namespace {
 
 constexpr int kT = 128;                                    // vertices per tile = threads per block
+constexpr int kBlocksPerSm = 4;                            // persistent blocks per SM
 
 __device__ __forceinline__ void bf16x8_to_f32(uint4 q, float *f) {
   const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&q);
@@ -578,7 +579,10 @@ int ensure_mpnn(bl_ctx *ctx, int n) {
     BL_CUDA(ctx, cudaMalloc(&m.adam_m, sizeof(float) * kMpnnParams));
     BL_CUDA(ctx, cudaMalloc(&m.adam_s, sizeof(float) * kMpnnParams));
     BL_CUDA(ctx, cudaMalloc(&m.wbf, sizeof(__nv_bfloat16) * kMpnnParams));
-    m.grid = ctx->num_sms * 2;
+    // four resident 128-thread blocks per SM (48 KB of shared memory and 64
+    // tensor-memory columns each): the layers' neighbour gathers are
+    // latency-bound, and two blocks per SM left 88 % of the warp slots empty
+    m.grid = ctx->num_sms * kBlocksPerSm;
     BL_CUDA(ctx, cudaMalloc(&m.part, sizeof(float) * (size_t)m.grid * (64 * 128 + 64)));
     BL_CUDA(ctx, cudaMalloc(&m.loss_part, sizeof(double) * m.grid));
     if (!ctx->s.status) {
