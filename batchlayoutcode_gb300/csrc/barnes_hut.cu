@@ -575,7 +575,15 @@ struct TreeArgs {
   int *startcnt;
   int *qpar;     // quad parent of internal node i (index i) and of leaf k (index n-1+k); -1 for the root
   int *qnchild;  // children of a quad node
-  int *qarrive;  // children whose centroid is done (zero before the pass)
+  // quad nodes whose range spans centroid blocks, by level (0..32):
+  // span_cnt[level] (zero before the pass), span_list[level * span_cap + slot]
+  int *span_cnt;
+  int *span_list;
+  int span_cap;
+  int *span_pos;  // position of a listed node (span_stage_kernel)
+  double2 *stage_val;  // staged listed nodes (span_stage_kernel -> centroid_top_kernel)
+  int4 *stage_pend;
+  int2 *stage_meta;
   const int4 *bnode;  // packed internal nodes, two int4 each (radix_tree_kernel)
   DevStatus *st;
 };
@@ -669,22 +677,30 @@ __global__ void __launch_bounds__(256) chain_kernel(TreeArgs t) {
   t.startcnt[k] = cnt;
 }
 
-// Centroids bottom-up, without grid barriers or waits.  The centroid of a
-// quad node is the unweighted mean of its children summed in quadrant order
-// in FP64 (BarnesHut.h:197-217), bit-identical to the reference; it can be
-// computed once every child is done.  A block owns kCenSpan consecutive
-// sorted points; a binary node whose range lies inside them has its index
-// there too (a Karras node's index is one of its range ends), so the block
-// loads those nodes' structure and its points into shared memory with
-// coalesced reads, and processes the nodes in rounds: the nodes whose
+// Centroids bottom-up in two launches.  The centroid of a quad node is the
+// unweighted mean of its children summed in quadrant order in FP64
+// (BarnesHut.h:197-217), bit-identical to the reference; it can be computed
+// once every child is done.  centroid_kernel: a block owns kCenSpan
+// consecutive sorted points; a binary node whose range lies inside them has
+// its index there too (a Karras node's index is one of its range ends), so
+// the block loads those nodes' structure and its points into shared memory
+// with coalesced reads, and processes the nodes in rounds: the nodes whose
 // children are all done form a queue, handled one node per thread so that the
 // FP64 work (a small fraction of the FP32 rate on this part, charged per warp
 // instruction) runs in full warps, and a node's last arriving child appends
-// it to the next round's queue.  A node that spans blocks is computed by the
-// thread whose arrival at it (device-scope acquire-release counter) is the
-// last, which climbs on from there: such nodes are few.
+// it to the next round's queue.  A quad node whose range spans blocks is only
+// listed, by level.  span_stage_kernel gathers the listed nodes' children
+// over the whole device; centroid_top_kernel, one thread-block cluster,
+// computes the listed nodes level by level from the deepest, a cluster
+// barrier between levels — a node's children are one level deeper at least,
+// so each level finds its children done.  (This replaced a climb by the last
+// arriving child through device-scope counters: one serial chain of L2 round
+// trips per level, 58 us of the pass on a 1M-point tree against 40 us now.)  At one level the quad nodes' ranges are disjoint
+// and a spanning one contains a block boundary, so a level lists fewer nodes
+// than there are blocks.
 constexpr int kCenThreads = 512;
 constexpr int kCenSpan = 1024;  // sorted points per block
+constexpr int kQuadLevels = 33;  // quad levels 0..31, 32 for runs of identical keys
 
 struct CenSmem {
   double2 cen[kCenSpan];
@@ -699,52 +715,50 @@ struct CenSmem {
   int qn[2];
 };
 
-// Arrival at a node that spans blocks; the last arrival computes it and
-// climbs on (bounded by the tree height).  Everything is read from global
-// memory: every child's writer arrived with release semantics.
-__device__ void climb_spanning(const TreeArgs &t, int node) {
-  while (node >= 0) {
-    const int need = t.qnchild[node];
-    const int up = t.qpar[node];
-    const int p = t.dlt[node];
+__device__ __forceinline__ int quad_level(int p) { return p >= 64 ? 32 : (p >> 1); }
+
+// Centroid of quad node `node` from global memory: its children's centroids
+// were written by an earlier launch or before the last cluster barrier (read
+// through L2).
+__device__ double2 quad_centroid_global(const TreeArgs &t, int node) {
+  double cx = 0.0, cy = 0.0;
+  int cnt = 0;
+  if (t.dlt[node] >= 64) {
+    const int2 rg = t.range[node];
+    for (int q = rg.x; q <= rg.y; q++) {
+      const float2 v = t.spos[q];
+      cx = cnt ? __dadd_rn(cx, f2d_int(v.x)) : zero_plus(f2d_int(v.x));
+      cy = cnt ? __dadd_rn(cy, f2d_int(v.y)) : zero_plus(f2d_int(v.y));
+      cnt++;
+    }
+  } else {
     const int4 kk = t.qkids[node];
-    int old;
-    asm volatile("atom.add.acq_rel.gpu.s32 %0, [%1], 1;" : "=r"(old) : "l"(&t.qarrive[node]) : "memory");
-    if (old != need - 1) return;
-    double cx = 0.0, cy = 0.0;
-    int cnt = 0;
-    if (p >= 64) {
-      const int2 rg = t.range[node];
-      for (int q = rg.x; q <= rg.y; q++) {
-        const float2 v = t.spos[q];
-        cx = cnt ? __dadd_rn(cx, f2d_int(v.x)) : zero_plus(f2d_int(v.x));
-        cy = cnt ? __dadd_rn(cy, f2d_int(v.y)) : zero_plus(f2d_int(v.y));
-        cnt++;
-      }
-    } else {
-      const int kids[4] = {kk.x, kk.y, kk.z, kk.w};
+    const int kids[4] = {kk.x, kk.y, kk.z, kk.w};
+    double vx[4], vy[4];
 #pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const int ch = kids[c];
-        if (ch == kNoChild) break;
-        double vx, vy;
-        if (ch < 0) {
-          const float2 v = t.spos[~ch];
-          vx = f2d_int(v.x);
-          vy = f2d_int(v.y);
-        } else {
-          const double2 v = __ldcg(&t.qcen[ch]);
-          vx = v.x;
-          vy = v.y;
-        }
-        cx = c ? __dadd_rn(cx, vx) : zero_plus(vx);
-        cy = c ? __dadd_rn(cy, vy) : zero_plus(vy);
-        cnt++;
+    for (int c = 0; c < 4; c++) {  // the loads first, then the ordered sum
+      const int ch = kids[c];
+      vx[c] = vy[c] = 0.0;
+      if (ch == kNoChild) continue;
+      if (ch < 0) {
+        const float2 v = t.spos[~ch];
+        vx[c] = f2d_int(v.x);
+        vy[c] = f2d_int(v.y);
+      } else {
+        const double2 v = __ldcg(&t.qcen[ch]);
+        vx[c] = v.x;
+        vy[c] = v.y;
       }
     }
-    t.qcen[node] = make_double2(div_count_int(cx, cnt), div_count_int(cy, cnt));
-    node = up;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      if (kids[c] == kNoChild) break;
+      cx = c ? __dadd_rn(cx, vx[c]) : zero_plus(vx[c]);
+      cy = c ? __dadd_rn(cy, vy[c]) : zero_plus(vy[c]);
+      cnt++;
+    }
   }
+  return make_double2(div_count_int(cx, cnt), div_count_int(cy, cnt));
 }
 
 __global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
@@ -768,6 +782,11 @@ __global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
         S.kids[q] = t.qkids[j];
         S.dlt[q] = t.dlt[j];
         S.par[q] = t.qpar[j];
+      } else if (m > 0) {  // spans blocks: computed by centroid_top_kernel
+        const int lvl = quad_level(t.dlt[j]);
+        const int slot = atomicAdd(&t.span_cnt[lvl], 1);
+        if (slot < t.span_cap) t.span_list[lvl * t.span_cap + slot] = j;
+        else dev_record_error(t.st, DEV_BAD_INDEX);  // cannot happen (see above)
       }
     }
     S.need[q] = (unsigned short)need;
@@ -778,12 +797,8 @@ __global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
   // round 0: every point arrives at its quad parent
   for (int k = lo + tid; k < hi; k += kCenThreads) {
     const int par = S.leafpar[k - lo];
-    if (par < 0) continue;
-    if (is_local(par)) {
-      if (atomicAdd(&S.arrive[par - lo], 1) == (int)S.need[par - lo] - 1) S.queue[0][atomicAdd(&S.qn[0], 1)] = par;
-    } else {
-      climb_spanning(t, par);
-    }
+    if (par < 0 || !is_local(par)) continue;  // a spanning parent is listed by its own block
+    if (atomicAdd(&S.arrive[par - lo], 1) == (int)S.need[par - lo] - 1) S.queue[0][atomicAdd(&S.qn[0], 1)] = par;
   }
   __syncthreads();
   // rounds: the ready local nodes, one per thread (bounded by the depth of
@@ -834,16 +849,240 @@ __global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
       S.cen[ln] = c2;
       t.qcen[node] = c2;
       const int up = S.par[ln];
-      if (up < 0) continue;
-      if (is_local(up)) {
-        if (atomicAdd(&S.arrive[up - lo], 1) == (int)S.need[up - lo] - 1)
-          S.queue[cur ^ 1][atomicAdd(&S.qn[cur ^ 1], 1)] = up;
-      } else {
-        climb_spanning(t, up);  // releases this node's centroid first
-      }
+      if (up < 0 || !is_local(up)) continue;
+      if (atomicAdd(&S.arrive[up - lo], 1) == (int)S.need[up - lo] - 1)
+        S.queue[cur ^ 1][atomicAdd(&S.qn[cur ^ 1], 1)] = up;
     }
     __syncthreads();
   }
+}
+
+constexpr int kTopCtas = 8;  // one cluster (the portable maximum size)
+constexpr int kTopThreads = 1024;
+constexpr int kTopCap = 2048;  // listed nodes per block held in shared memory
+constexpr int kStageThreads = 128;
+
+__device__ __forceinline__ void top_cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned int top_cluster_rank() {
+  unsigned int r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// v = the double2 at `p` in the shared memory of block `rank` of the cluster.
+__device__ __forceinline__ double2 ld_cluster_double2(const double2 *p, unsigned int rank) {
+  const unsigned int a = (unsigned int)__cvta_generic_to_shared(p);
+  unsigned int ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  double x, y;
+  asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(x), "=d"(y) : "r"(ra));
+  return make_double2(x, y);
+}
+
+// Position g of a listed node: level lvl's nodes follow the deeper levels'
+// (off[lvl] = the deeper levels' count), node q of a level at g = off + q.
+// In the cluster, block g % kTopCtas holds it in slot g / kTopCtas; its staged
+// record sits at (g % kTopCtas) * kTopCap + g / kTopCtas.
+struct SpanLevels {
+  int cnt[kQuadLevels], off[kQuadLevels], total;
+};
+
+// Every thread of the block calls it.
+__device__ __forceinline__ void span_levels(const TreeArgs &t, SpanLevels &L) {
+  if (threadIdx.x < kQuadLevels) L.cnt[threadIdx.x] = max(0, min(t.span_cnt[threadIdx.x], t.span_cap));
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int o = 0;
+    for (int lvl = kQuadLevels - 1; lvl >= 0; lvl--) {
+      L.off[lvl] = o;
+      o += L.cnt[lvl];
+    }
+    L.total = o;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ int span_level_of(const SpanLevels &L, int g) {
+  int lvl = 0;
+  while (lvl < kQuadLevels - 1 && g < L.off[lvl]) lvl++;
+  return lvl;
+}
+
+// Staging of the listed nodes, one thread each, over the whole device (the
+// gathers of a node's children are scattered loads; on the cluster's few SMs
+// alone they queue): the node's position, and per child its centroid when it
+// is final (a point, or a node inside one block) or its node id when it is a
+// listed node itself.  A run of identical keys (children: points only) is
+// computed here.  Nothing is staged when the cluster cannot hold the nodes.
+__global__ void __launch_bounds__(kStageThreads) span_stage_kernel(TreeArgs t) {
+  __shared__ SpanLevels L;
+  if (!block_status_ok(t.st)) return;
+  span_levels(t, L);
+  const int total = L.total;
+  const int g = blockIdx.x * kStageThreads + threadIdx.x;
+  if (total > kTopCtas * kTopCap || g >= total) return;
+  const int lvl = span_level_of(L, g);
+  const int idx = (g % kTopCtas) * kTopCap + g / kTopCtas;
+  const int node = t.span_list[lvl * t.span_cap + (g - L.off[lvl])];
+  if (node < 0 || node >= t.n - 1) {
+    dev_record_error(t.st, DEV_BAD_INDEX);
+    t.stage_meta[idx] = make_int2(-1, 0);
+    t.stage_pend[idx] = make_int4(-1, -1, -1, -1);
+    t.stage_val[idx] = make_double2(0.0, 0.0);
+    return;
+  }
+  t.span_pos[node] = g;
+  const int p = t.dlt[node];
+  const int4 kk = t.qkids[node];
+  if (p >= 64) {  // a run
+    t.stage_val[idx] = quad_centroid_global(t, node);
+    t.stage_meta[idx] = make_int2(node, 0);
+    t.stage_pend[idx] = make_int4(-1, -1, -1, -1);
+    return;
+  }
+  const int kids[4] = {kk.x, kk.y, kk.z, kk.w};
+  int2 rg[4];
+  double2 qc[4];
+  float2 pt[4];
+#pragma unroll
+  for (int c = 0; c < 4; c++) {  // independent loads issued together
+    const int ch = kids[c];
+    rg[c] = make_int2(0, 0);
+    qc[c] = make_double2(0.0, 0.0);
+    pt[c] = make_float2(0.f, 0.f);
+    if (ch == kNoChild) continue;
+    if (ch < 0) {
+      pt[c] = t.spos[~ch];
+    } else {
+      rg[c] = t.range[ch];
+      qc[c] = __ldcg(&t.qcen[ch]);  // used only when the child is inside one block
+    }
+  }
+  int pend[4] = {-1, -1, -1, -1};
+  int nc = 0;
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    const int ch = kids[c];
+    if (ch == kNoChild) break;
+    nc++;
+    double2 v = make_double2(0.0, 0.0);
+    if (ch < 0) v = make_double2(f2d_int(pt[c].x), f2d_int(pt[c].y));
+    else if (rg[c].x / kCenSpan != rg[c].y / kCenSpan) pend[c] = ch;  // listed
+    else v = qc[c];
+    t.stage_val[(size_t)c * kTopCtas * kTopCap + idx] = v;
+  }
+  t.stage_pend[idx] = make_int4(pend[0], pend[1], pend[2], pend[3]);
+  t.stage_meta[idx] = make_int2(node, nc);
+}
+
+struct TopSmem {
+  double2 val[4][kTopCap];  // the children's centroids in quadrant order
+  double2 cen[kTopCap];     // the node's centroid (read by the other blocks)
+  int4 pend[kTopCap];       // cluster position of a listed child, -1 otherwise
+  int node[kTopCap];
+  int nc[kTopCap];          // children; 0 for a run (done when staged) or a bad entry
+};
+
+// The listed nodes, level by level from the deepest, in one cluster: each
+// block loads its staged records and the positions of their listed children,
+// then one level per round, a listed child read from the shared memory of the
+// block holding it, a cluster barrier after every round.  Every thread reads
+// the same level counts, so all take the same cluster barriers; every block
+// reads the error record before the first barrier and this kernel records
+// errors only after it, so all blocks leave together or none.  More listed
+// nodes than the blocks can hold: the same rounds through global memory.
+__global__ void __cluster_dims__(kTopCtas, 1, 1) __launch_bounds__(kTopThreads, 1)
+    centroid_top_kernel(TreeArgs t) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TopSmem &S = *reinterpret_cast<TopSmem *>(smem_raw);
+  __shared__ SpanLevels L;
+  __shared__ unsigned int s_code;
+  const int tid = threadIdx.x;
+  if (tid == 0) s_code = ld_volatile_u32(&t.st->code);
+  top_cluster_sync();
+  if (s_code != 0u) return;  // the tree of this iteration is not valid
+  span_levels(t, L);
+  const int total = L.total;
+  if (total > kTopCtas * kTopCap) {
+    for (int lvl = kQuadLevels - 1; lvl >= 0; lvl--) {
+      const int cnt = L.cnt[lvl];
+      if (cnt == 0) continue;
+      for (int q = blockIdx.x * kTopThreads + tid; q < cnt; q += kTopCtas * kTopThreads) {
+        const int node = t.span_list[lvl * t.span_cap + q];
+        if (node < 0 || node >= t.n - 1) {
+          dev_record_error(t.st, DEV_BAD_INDEX);
+          continue;
+        }
+        t.qcen[node] = quad_centroid_global(t, node);
+      }
+      top_cluster_sync();
+    }
+    return;
+  }
+  const int crank = (int)top_cluster_rank();
+  const int nslots = total > crank ? (total - crank + kTopCtas - 1) / kTopCtas : 0;
+  for (int l = tid; l < nslots; l += kTopThreads) {
+    const int idx = crank * kTopCap + l;
+    const int2 meta = t.stage_meta[idx];
+    const int4 pk = t.stage_pend[idx];
+    int pend[4] = {pk.x, pk.y, pk.z, pk.w};
+    int gc[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) gc[c] = pend[c] >= 0 ? __ldcg(&t.span_pos[pend[c]]) : -1;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      if (pend[c] >= 0 && (gc[c] < 0 || gc[c] >= total)) {
+        dev_record_error(t.st, DEV_BAD_INDEX);
+        gc[c] = -1;
+      }
+      S.val[c][l] = t.stage_val[(size_t)c * kTopCtas * kTopCap + idx];
+    }
+    S.pend[l] = make_int4(gc[0], gc[1], gc[2], gc[3]);
+    S.node[l] = meta.x;
+    S.nc[l] = meta.y;
+    if (meta.y == 0) S.cen[l] = S.val[0][l];  // a run (or a bad entry: zero)
+  }
+  top_cluster_sync();  // every block's staged records (and runs) in place
+  // this thread's positions of level lvl: g = first + k * kTopCtas * kTopThreads
+  auto first_of = [&](int lvl) {
+    const int off = L.off[lvl];
+    return off + (crank - off % kTopCtas + kTopCtas) % kTopCtas + kTopCtas * tid;
+  };
+  // the rounds (runs, level 32, were done when staged)
+  for (int lvl = kQuadLevels - 2; lvl >= 0; lvl--) {
+    if (L.cnt[lvl] == 0) continue;
+    const int end = L.off[lvl] + L.cnt[lvl];
+    for (int g = first_of(lvl); g < end; g += kTopCtas * kTopThreads) {
+      const int l = g / kTopCtas;
+      const int nc = S.nc[l];
+      if (nc == 0) continue;
+      const int4 pk = S.pend[l];
+      const int pend[4] = {pk.x, pk.y, pk.z, pk.w};
+      double2 v[4];
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        v[c] = S.val[c][l];
+        if (c < nc && pend[c] >= 0) v[c] = ld_cluster_double2(&S.cen[pend[c] / kTopCtas], pend[c] % kTopCtas);
+      }
+      double cx = 0.0, cy = 0.0;
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        if (c >= nc) break;
+        cx = c ? __dadd_rn(cx, v[c].x) : zero_plus(v[c].x);
+        cy = c ? __dadd_rn(cy, v[c].y) : zero_plus(v[c].y);
+      }
+      S.cen[l] = make_double2(div_count_int(cx, nc), div_count_int(cy, nc));
+    }
+    // no global store is pending here, so the barrier's release has only
+    // this round's shared-memory stores to order; it also keeps every
+    // block's shared memory alive while the others read it
+    top_cluster_sync();
+  }
+  for (int l = tid; l < nslots; l += kTopThreads)
+    if (S.node[l] >= 0) t.qcen[S.node[l]] = S.cen[l];
 }
 
 struct LayoutArgs {
@@ -1151,7 +1390,7 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   auto fr = [](void *p) { if (p) cudaFree(p); };
   fr(s.keys); fr(s.keys_alt); fr(s.perm); fr(s.perm_alt); fr(s.hist); fr(s.spos);
   fr(s.bparent); fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.qkids); fr(s.qpar); fr(s.qnchild);
-  fr(s.qarrive); fr(s.qcen);
+  fr(s.span); fr(s.span_stage); fr(s.qcen);
   fr(s.qbelow); fr(s.startcnt); fr(s.startbase); fr(s.nodes); fr(s.nodes_c64);
   fr(s.nodes_lvl); fr(s.rep); fr(s.f0); fr(s.pos_alt); fr(s.runs); fr(s.bnode);
   const size_t nb = (n + kRsTile - 1) / kRsTile;
@@ -1171,7 +1410,10 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   BL_CUDA(ctx, cudaMalloc(&s.qkids, m * sizeof(int4)));
   BL_CUDA(ctx, cudaMalloc(&s.qpar, 2 * m * sizeof(int)));
   BL_CUDA(ctx, cudaMalloc(&s.qnchild, m * sizeof(int)));
-  BL_CUDA(ctx, cudaMalloc(&s.qarrive, m * sizeof(int)));
+  s.span_cap = nblk((long long)m, kCenSpan);
+  BL_CUDA(ctx, cudaMalloc(&s.span, (kQuadLevels + (size_t)kQuadLevels * s.span_cap + m) * sizeof(int)));
+  BL_CUDA(ctx, cudaMalloc(&s.span_stage, (size_t)kTopCtas * kTopCap * (4 * sizeof(double2) + sizeof(int4) +
+                                                                        sizeof(int2))));
   BL_CUDA(ctx, cudaMalloc(&s.qcen, m * sizeof(double2)));
   BL_CUDA(ctx, cudaMalloc(&s.qbelow, m * sizeof(int)));
   BL_CUDA(ctx, cudaMalloc(&s.startcnt, (m + 1) * sizeof(int)));
@@ -1191,6 +1433,8 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   // set here, outside any stream capture of the iteration
   BL_CUDA(ctx, cudaFuncSetAttribute(centroid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)sizeof(CenSmem)));
+  BL_CUDA(ctx, cudaFuncSetAttribute(centroid_top_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sizeof(TopSmem)));
   s.bh_n = n;
   return 0;
 }
@@ -1249,7 +1493,7 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
   radix_tree_kernel<<<nblk(n - 1, 256), 256, 0, st>>>(s.keys, n, s.bchild, s.brange, s.bdelta, s.bparent,
                                                        reinterpret_cast<int *>(s.bnode));
   bl_time_end(ctx, "gather_tree");
-  BL_CUDA(ctx, cudaMemsetAsync(s.qarrive, 0, (size_t)n * sizeof(int), st));
+  BL_CUDA(ctx, cudaMemsetAsync(s.span, 0, kQuadLevels * sizeof(int), st));
   BL_CUDA(ctx, cudaMemsetAsync(s.startcnt + n, 0, sizeof(int), st));
   TreeArgs t;
   t.n = n;
@@ -1264,7 +1508,13 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
   t.startcnt = s.startcnt;
   t.qpar = s.qpar;
   t.qnchild = s.qnchild;
-  t.qarrive = s.qarrive;
+  t.span_cnt = s.span;
+  t.span_list = s.span + kQuadLevels;
+  t.span_cap = s.span_cap;
+  t.span_pos = s.span + kQuadLevels + (size_t)kQuadLevels * s.span_cap;
+  t.stage_val = reinterpret_cast<double2 *>(s.span_stage);
+  t.stage_pend = reinterpret_cast<int4 *>(t.stage_val + 4 * kTopCtas * kTopCap);
+  t.stage_meta = reinterpret_cast<int2 *>(t.stage_pend + kTopCtas * kTopCap);
   t.bnode = s.bnode;
   t.st = s.status;
   bl_time_begin(ctx, "chain_kernel");
@@ -1272,6 +1522,13 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
   bl_time_end(ctx, "chain_kernel");
   bl_time_begin(ctx, "centroid_kernel");
   centroid_kernel<<<nblk(n, kCenSpan), kCenThreads, sizeof(CenSmem), st>>>(t);
+  bl_time_begin(ctx, "centroid_top");
+  if (nblk(n, kCenSpan) > 1) {  // one block has no spanning node
+    span_stage_kernel<<<kTopCtas * kTopCap / kStageThreads, kStageThreads, 0, st>>>(t);
+    centroid_top_kernel<<<kTopCtas, kTopThreads, sizeof(TopSmem), st>>>(t);
+    ctx->launches += 2;
+  }
+  bl_time_end(ctx, "centroid_top");
   bl_time_end(ctx, "centroid_kernel");
   ctx->launches += 4;
   bl_time_begin(ctx, "scan_layout");

@@ -209,7 +209,9 @@ struct Scratch {
   int4 *qkids = nullptr;         // quad children of a quad node
   int *qpar = nullptr;           // quad parent of a quad node / leaf
   int *qnchild = nullptr;        // number of children of a quad node
-  int *qarrive = nullptr;        // children finished (bottom-up centroid pass)
+  int *span = nullptr;           // centroid pass: spanning quad nodes per level (counts, then lists)
+  int span_cap = 0;              // list slots per level (centroid blocks)
+  void *span_stage = nullptr;    // staged spanning nodes for the cluster pass
   double2 *qcen = nullptr;       // centroid of quad node (indexed by binary internal id)
   int *qbelow = nullptr;         // chain length below a quad node
   int *startcnt = nullptr;       // quad nodes starting at each sorted position (n+1)

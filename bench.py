@@ -626,8 +626,8 @@ def run_batched(args, w, ws, rank, local):
 
 # Labels the library times with CUDA events around each stage of a
 # Barnes-Hut iteration (direct launches, not the replayed graph).
-BH_STAGES = ["frame_morton", "lsd_passes", "radix_sort", "gather_tree", "chain_kernel", "centroid_kernel",
-             "scan_layout", "traverse_kernel", "sweep_kernel"]
+BH_STAGES = ["frame_morton", "lsd_passes", "radix_sort", "gather_tree", "chain_kernel", "centroid_top",
+             "centroid_kernel", "scan_layout", "traverse_kernel", "sweep_kernel"]
 
 
 def stage_times(a, w, flush, steps, warmup):
@@ -663,8 +663,9 @@ def stage_times(a, w, flush, steps, warmup):
             ts.append(a.last_run_ms())
         ts = sorted(ts[2:])
         out["graph_iteration" if mode else "direct_iteration"] = round(sum(ts) / len(ts) * 1000, 1)
-    out["note"] = ("lsd_passes is part of radix_sort (which adds the runs of equal high halves); "
-                   "the stages of a direct iteration add up to direct_iteration")
+    out["note"] = ("lsd_passes is part of radix_sort (which adds the runs of equal high halves), centroid_top "
+                   "(the nodes that span blocks) part of centroid_kernel; the other stages of a direct "
+                   "iteration add up to direct_iteration")
     return out
 
 
