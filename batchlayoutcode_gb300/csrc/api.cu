@@ -173,7 +173,7 @@ void free_ctx(bl_ctx *c) {
   fr(s.energy_parts); fr(s.energy); fr(s.status); fr(s.partials); fr(s.keys); fr(s.keys_alt);
   fr(s.perm); fr(s.perm_alt); fr(s.hist); fr(s.bbox); fr(s.frame); fr(s.spos); fr(s.bparent);
   fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.qkids); fr(s.qpar); fr(s.qnchild); fr(s.span); fr(s.span_stage); fr(s.qcen); fr(s.qbelow); fr(s.startcnt);
-  fr(s.startbase); fr(s.scan_tmp); fr(s.nodes); fr(s.nodes_c64); fr(s.nodes_lvl); fr(s.rep);
+  fr(s.startbase); fr(s.nodes); fr(s.nodes_c64); fr(s.nodes_lvl); fr(s.rep);
   fr(s.stats); fr(s.pos_alt); fr(s.f0); fr(s.runs); fr(s.bnode); fr(s.cursor); fr(s.cursor_full); fr(s.walk_off); fr(s.walk_pairs);
   fr(s.term_off); fr(s.terms); fr(s.term_tgt); fr(s.greedy_share); fr(s.greedy_pos);
   for (auto &ls : c->schedules) {
@@ -191,6 +191,9 @@ void free_ctx(bl_ctx *c) {
   for (auto ev : c->ev_pool) cudaEventDestroy(ev);
   for (auto ev : c->run_ev)
     if (ev) cudaEventDestroy(ev);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -309,8 +312,16 @@ bl_ctx *bl_algorithms_create(int device, int n, long long nnz, const int *rowptr
   if (e != cudaSuccess) return bad(e, "cudaSetDevice");
   ctx->device = device;
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
-  e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  // the main stream at the highest priority: work beside it on `side` (the
+  // lowest) gives way to it
+  int prio_least = 0, prio_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+  e = cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, prio_greatest);
   if (e != cudaSuccess) return bad(e, "cudaStreamCreate");
+  e = cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, prio_least);
+  if (e != cudaSuccess) return bad(e, "cudaStreamCreate");
+  if ((e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming)) != cudaSuccess) return bad(e, "cudaEventCreate");
+  if ((e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming)) != cudaSuccess) return bad(e, "cudaEventCreate");
   ctx->input = input ? input : "";
   ctx->outputdir = outputdir ? outputdir : "";
   ctx->initfile = initfile ? initfile : "";

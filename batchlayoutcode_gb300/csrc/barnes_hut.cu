@@ -583,24 +583,26 @@ struct TreeArgs {
   int *span_pos;  // position of a listed node (span_stage_kernel)
   double2 *stage_val;  // staged listed nodes (span_stage_kernel -> centroid_top_kernel)
   int4 *stage_pend;
-  int2 *stage_meta;
+  int4 *stage_meta;
+  // pre-order records: quad nodes starting before each centroid block
+  // (chain_kernel adds them up, block_base_kernel turns them into offsets),
+  // startbase[k] = quad nodes starting before sorted position k
+  int *blocktot;
+  int *startbase;
+  const double *frame;
+  double inv_theta2;  // 1 / theta^2, folded into the records' z
+  float4 *nodes;
+  double2 *nodes_c64;
+  unsigned char *nodes_lvl;
   const int4 *bnode;  // packed internal nodes, two int4 each (radix_tree_kernel)
   DevStatus *st;
 };
 
 constexpr int kNoChild = INT_MIN;
+constexpr int kCenSpanC = 1024;  // sorted points per centroid block
 
+__device__ __forceinline__ int quad_level(int p) { return p >= 64 ? 32 : (p >> 1); }
 
-// Internal node merged into its parent's quad node: the x-bit split of the
-// digit whose y-bit split is the parent, or any split inside a run of equal
-// keys below its top.
-__device__ __forceinline__ bool is_sub(const TreeArgs &t, int node) {
-  if (node <= 0) return false;
-  const int p = t.dlt[node];
-  const int pp = t.dlt[t.parent[node]];
-  if (p >= 64) return pp >= 64;
-  return (p & 1) && (pp == p - 1);
-}
 
 // Structure of the quadtree, one thread per sorted position k.  The binary
 // nodes whose range starts at k form the left-child chain above leaf k; the
@@ -609,9 +611,17 @@ __device__ __forceinline__ bool is_sub(const TreeArgs &t, int node) {
 // number of quad nodes below it on the chain (qbelow), its quad children, their
 // count, and itself as their quad parent; startcnt[k] counts the quad nodes
 // starting at k.
+__device__ __forceinline__ int chain_walk(const TreeArgs &t, int k);
+
 __global__ void __launch_bounds__(256) chain_kernel(TreeArgs t) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= t.n) return;
+  const int cnt = k < t.n ? chain_walk(t, k) : 0;
+  // quad nodes starting in this warp's 32 positions (one centroid block)
+  const int sum = __reduce_add_sync(0xffffffffu, cnt);
+  if ((threadIdx.x & 31) == 0 && sum) atomicAdd(&t.blocktot[(k & ~31) / kCenSpanC], sum);
+}
+
+__device__ __forceinline__ int chain_walk(const TreeArgs &t, int k) {
   int cnt = 0;
   int cur = t.parent[t.n - 1 + k];
   if (k == 0) t.qpar[0] = -1;  // the root
@@ -675,6 +685,82 @@ __global__ void __launch_bounds__(256) chain_kernel(TreeArgs t) {
     rb = pb;
   }
   t.startcnt[k] = cnt;
+  return cnt;
+}
+
+// Exclusive offsets of the centroid blocks' quad-node counts, in place
+// (tot[nb] = the number of quad nodes), and startbase[n] = the same.  One
+// block of 1024 threads.
+__global__ void __launch_bounds__(1024) block_base_kernel(int *tot, int nb, int *startbase_n) {
+  __shared__ int ws[32];
+  __shared__ int carry;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  if (tid == 0) carry = 0;
+  __syncthreads();
+  for (int c0 = 0; c0 < nb; c0 += 1024) {
+    const int b = c0 + tid;
+    const int v = b < nb ? tot[b] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    int wpre = 0, total = 0;
+    for (int q = 0; q < 32; q++) {
+      const int u = ws[q];
+      if (q < w) wpre += u;
+      total += u;
+    }
+    const int base = carry;
+    if (b < nb) tot[b] = base + wpre + x - v;
+    __syncthreads();
+    if (tid == 0) carry = base + total;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    tot[nb] = carry;
+    *startbase_n = carry;
+  }
+}
+
+// Pre-order record of quad node `node` (BarnesHut.h:114-225 as a flat walk):
+// the record after the quad nodes starting before position lo = range.x and
+// the deeper quad nodes starting at lo; its skip link is the first record
+// after its range.  sc_lo = quad nodes starting at lo, sb_lo / sb_hi =
+// startbase at lo and at hi = range.y + 1, qb = quad nodes below it starting
+// at lo.  False (and DEV_BAD_INDEX) for offsets that cannot be.
+__device__ __forceinline__ bool node_record_slot(const TreeArgs &t, int lo, int hi, int qb, int sc_lo, int sb_lo,
+                                                 int sb_hi, int &idx, int &skip) {
+  const int cap = 2 * t.n - 1;  // records: n leaves + at most n-1 quad nodes
+  const int rank = sc_lo - 1 - qb;
+  idx = lo + sb_lo + rank;
+  skip = hi + sb_hi;
+  if (rank < 0 || idx < 0 || idx >= cap || skip <= idx || skip > cap) {
+    dev_record_error(t.st, DEV_BAD_INDEX);
+    return false;
+  }
+  return true;
+}
+
+// {x, y, D^2 / theta^2, skip} with the FP64 centroid and the level beside it
+// (the walk's FP64 re-test reads those two).
+__device__ __forceinline__ void write_node_record(const TreeArgs &t, int idx, int skip, int lvl, double2 c) {
+  const double D = ldexp(t.frame[2], -lvl);
+  t.nodes[idx] = make_float4(d2f_int(c.x), d2f_int(c.y), bh_record_z(D, t.inv_theta2), __int_as_float(skip));
+  t.nodes_c64[idx] = c;
+  t.nodes_lvl[idx] = (unsigned char)lvl;
+}
+
+// The same from global memory (startbase of the whole range written).
+__device__ __forceinline__ void write_node_record_global(const TreeArgs &t, int node, double2 c) {
+  const int2 rg = t.range[node];
+  int idx, skip;
+  if (node_record_slot(t, rg.x, rg.y + 1, t.qbelow[node], t.startcnt[rg.x], t.startbase[rg.x],
+                       t.startbase[rg.y + 1], idx, skip))
+    write_node_record(t, idx, skip, quad_level(t.dlt[node]), c);
 }
 
 // Centroids bottom-up in two launches.  The centroid of a quad node is the
@@ -699,7 +785,7 @@ __global__ void __launch_bounds__(256) chain_kernel(TreeArgs t) {
 // and a spanning one contains a block boundary, so a level lists fewer nodes
 // than there are blocks.
 constexpr int kCenThreads = 512;
-constexpr int kCenSpan = 1024;  // sorted points per block
+constexpr int kCenSpan = kCenSpanC;
 constexpr int kQuadLevels = 33;  // quad levels 0..31, 32 for runs of identical keys
 
 struct CenSmem {
@@ -714,8 +800,6 @@ struct CenSmem {
   unsigned short need[kCenSpan];  // children of the local quad node here (<= kCenSpan), 0 if none
   int qn[2];
 };
-
-__device__ __forceinline__ int quad_level(int p) { return p >= 64 ? 32 : (p >> 1); }
 
 // Centroid of quad node `node` from global memory: its children's centroids
 // were written by an earlier launch or before the last cluster barrier (read
@@ -855,6 +939,55 @@ __global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
     }
     __syncthreads();
   }
+  // startbase over the block (the round queues are free now): the blocks
+  // before it plus an exclusive scan of startcnt inside it
+  __syncthreads();
+  const int span = hi - lo;
+  const int q0 = 2 * tid, q1 = 2 * tid + 1;  // kCenSpan == 2 * kCenThreads
+  const int c0 = q0 < span ? t.startcnt[lo + q0] : 0, c1 = q1 < span ? t.startcnt[lo + q1] : 0;
+  const int bbase = t.blocktot[blockIdx.x];
+  int x = c0 + c1;
+  const int lane = tid & 31, w = tid >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  int *wsum = S.queue[0];
+  if (lane == 31) wsum[w] = x;
+  __syncthreads();
+  int wpre = 0;
+  for (int q = 0; q < w; q++) wpre += wsum[q];
+  const int excl = bbase + wpre + x - (c0 + c1);
+  if (q0 < span) t.startbase[lo + q0] = excl;
+  if (q1 < span) t.startbase[lo + q1] = excl + c0;
+}
+
+// Pre-order records of the points and of the quad nodes inside one centroid
+// block, one thread per sorted position (the nodes that span blocks are
+// written by centroid_top_kernel).  It runs beside the spanning nodes' pass.
+__global__ void __launch_bounds__(256) layout_local_kernel(TreeArgs t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!block_status_ok(t.st)) return;
+  const int cap = 2 * t.n - 1;  // records: n leaves + at most n-1 quad nodes
+  if (i < t.n) {  // leaf (sorted point) i
+    const int idx = i + t.startbase[i] + t.startcnt[i];
+    if (idx < 0 || idx >= cap) {
+      dev_record_error(t.st, DEV_BAD_INDEX);
+      return;
+    }
+    const float2 p = t.spos[i];
+    // a leaf's z = -inf is never in doubt: no FP64 centroid or level needed
+    t.nodes[idx] = make_float4(p.x, p.y, kLeafZ, __int_as_float(idx + 1));
+  }
+  if (i < t.n - 1 && t.qnchild[i] > 0) {  // a quad node (binary internal node i)
+    const int2 rg = t.range[i];
+    if (rg.x / kCenSpan != rg.y / kCenSpan) return;  // spans blocks
+    int idx, skip;
+    if (node_record_slot(t, rg.x, rg.y + 1, t.qbelow[i], t.startcnt[rg.x], t.startbase[rg.x],
+                         t.startbase[rg.y + 1], idx, skip))
+      write_node_record(t, idx, skip, quad_level(t.dlt[i]), t.qcen[i]);
+  }
 }
 
 constexpr int kTopCtas = 8;  // one cluster (the portable maximum size)
@@ -929,7 +1062,7 @@ __global__ void __launch_bounds__(kStageThreads) span_stage_kernel(TreeArgs t) {
   const int node = t.span_list[lvl * t.span_cap + (g - L.off[lvl])];
   if (node < 0 || node >= t.n - 1) {
     dev_record_error(t.st, DEV_BAD_INDEX);
-    t.stage_meta[idx] = make_int2(-1, 0);
+    t.stage_meta[idx] = make_int4(-1, 0, -1, 0);
     t.stage_pend[idx] = make_int4(-1, -1, -1, -1);
     t.stage_val[idx] = make_double2(0.0, 0.0);
     return;
@@ -937,9 +1070,17 @@ __global__ void __launch_bounds__(kStageThreads) span_stage_kernel(TreeArgs t) {
   t.span_pos[node] = g;
   const int p = t.dlt[node];
   const int4 kk = t.qkids[node];
+  const int2 nr = t.range[node];
+  const int qb = t.qbelow[node];
+  // its record's place (startbase of the whole range was written by centroid_kernel)
+  int ridx, skip;
+  if (!node_record_slot(t, nr.x, nr.y + 1, qb, t.startcnt[nr.x], t.startbase[nr.x], t.startbase[nr.y + 1], ridx,
+                        skip))
+    ridx = -1;
+  const int lvl8 = quad_level(p) << 8;
   if (p >= 64) {  // a run
     t.stage_val[idx] = quad_centroid_global(t, node);
-    t.stage_meta[idx] = make_int2(node, 0);
+    t.stage_meta[idx] = make_int4(node, lvl8, ridx, skip);
     t.stage_pend[idx] = make_int4(-1, -1, -1, -1);
     return;
   }
@@ -975,7 +1116,7 @@ __global__ void __launch_bounds__(kStageThreads) span_stage_kernel(TreeArgs t) {
     t.stage_val[(size_t)c * kTopCtas * kTopCap + idx] = v;
   }
   t.stage_pend[idx] = make_int4(pend[0], pend[1], pend[2], pend[3]);
-  t.stage_meta[idx] = make_int2(node, nc);
+  t.stage_meta[idx] = make_int4(node, nc | lvl8, ridx, skip);
 }
 
 struct TopSmem {
@@ -1016,7 +1157,9 @@ __global__ void __cluster_dims__(kTopCtas, 1, 1) __launch_bounds__(kTopThreads, 
           dev_record_error(t.st, DEV_BAD_INDEX);
           continue;
         }
-        t.qcen[node] = quad_centroid_global(t, node);
+        const double2 c = quad_centroid_global(t, node);
+        t.qcen[node] = c;  // read by the next levels
+        write_node_record_global(t, node, c);
       }
       top_cluster_sync();
     }
@@ -1026,7 +1169,7 @@ __global__ void __cluster_dims__(kTopCtas, 1, 1) __launch_bounds__(kTopThreads, 
   const int nslots = total > crank ? (total - crank + kTopCtas - 1) / kTopCtas : 0;
   for (int l = tid; l < nslots; l += kTopThreads) {
     const int idx = crank * kTopCap + l;
-    const int2 meta = t.stage_meta[idx];
+    const int4 meta = t.stage_meta[idx];
     const int4 pk = t.stage_pend[idx];
     int pend[4] = {pk.x, pk.y, pk.z, pk.w};
     int gc[4];
@@ -1042,8 +1185,8 @@ __global__ void __cluster_dims__(kTopCtas, 1, 1) __launch_bounds__(kTopThreads, 
     }
     S.pend[l] = make_int4(gc[0], gc[1], gc[2], gc[3]);
     S.node[l] = meta.x;
-    S.nc[l] = meta.y;
-    if (meta.y == 0) S.cen[l] = S.val[0][l];  // a run (or a bad entry: zero)
+    S.nc[l] = meta.y & 255;
+    if ((meta.y & 255) == 0) S.cen[l] = S.val[0][l];  // a run (or a bad entry: zero)
   }
   top_cluster_sync();  // every block's staged records (and runs) in place
   // this thread's positions of level lvl: g = first + k * kTopCtas * kTopThreads
@@ -1081,60 +1224,11 @@ __global__ void __cluster_dims__(kTopCtas, 1, 1) __launch_bounds__(kTopThreads, 
     // block's shared memory alive while the others read it
     top_cluster_sync();
   }
-  for (int l = tid; l < nslots; l += kTopThreads)
-    if (S.node[l] >= 0) t.qcen[S.node[l]] = S.cen[l];
-}
-
-struct LayoutArgs {
-  int n;
-  double inv_theta2;  // 1 / theta^2, folded into the records' z
-  DevStatus *st;
-  const float2 *spos;
-  const int2 *range;
-  const int *dlt;
-  const int *parent;
-  const double2 *qcen;
-  const int *qbelow;
-  const int *startcnt;
-  const int *startbase;  // exclusive scan of startcnt, n+1 entries
-  const double *frame;
-  float4 *nodes;
-  double2 *nodes_c64;
-  unsigned char *nodes_lvl;
-};
-
-__global__ void layout_kernel(LayoutArgs L, TreeArgs t) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (!block_status_ok(L.st)) return;
-  const double maxmin = L.frame[2];
-  const int cap = 2 * L.n - 1;  // records: n leaves + at most n-1 quad nodes
-  if (i < L.n) {  // leaf (sorted point) i
-    const int idx = i + L.startbase[i] + L.startcnt[i];
-    if (idx < 0 || idx >= cap) {
-      dev_record_error(L.st, DEV_BAD_INDEX);
-      return;
-    }
-    const float2 p = L.spos[i];
-    // a leaf's z = -inf is never in doubt: no FP64 centroid or level needed
-    L.nodes[idx] = make_float4(p.x, p.y, kLeafZ, __int_as_float(idx + 1));
-  }
-  if (i < L.n - 1 && !is_sub(t, i)) {  // quad node = binary internal node i
-    const int2 rg = L.range[i];
-    const int lo = rg.x, hi = rg.y + 1;
-    const int p = L.dlt[i];
-    const int lvl = p >= 64 ? 32 : (p >> 1);
-    const int rank = L.startcnt[lo] - 1 - L.qbelow[i];
-    const int idx = lo + L.startbase[lo] + rank;
-    const int skip = hi + L.startbase[hi];
-    if (rank < 0 || idx < 0 || idx >= cap || skip <= idx || skip > cap) {
-      dev_record_error(L.st, DEV_BAD_INDEX);
-      return;
-    }
-    const double D = ldexp(maxmin, -lvl);
-    const double2 c = L.qcen[i];
-    L.nodes[idx] = make_float4(d2f_int(c.x), d2f_int(c.y), bh_record_z(D, L.inv_theta2), __int_as_float(skip));
-    L.nodes_c64[idx] = c;
-    L.nodes_lvl[idx] = (unsigned char)lvl;
+  for (int l = tid; l < nslots; l += kTopThreads) {
+    const int4 meta = t.stage_meta[crank * kTopCap + l];
+    if (meta.x < 0) continue;
+    t.qcen[meta.x] = S.cen[l];  // every quad node's centroid stays readable by node id
+    if (meta.z >= 0) write_node_record(t, meta.z, meta.w, meta.y >> 8, S.cen[l]);
   }
 }
 
@@ -1411,9 +1505,9 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   BL_CUDA(ctx, cudaMalloc(&s.qpar, 2 * m * sizeof(int)));
   BL_CUDA(ctx, cudaMalloc(&s.qnchild, m * sizeof(int)));
   s.span_cap = nblk((long long)m, kCenSpan);
-  BL_CUDA(ctx, cudaMalloc(&s.span, (kQuadLevels + (size_t)kQuadLevels * s.span_cap + m) * sizeof(int)));
-  BL_CUDA(ctx, cudaMalloc(&s.span_stage, (size_t)kTopCtas * kTopCap * (4 * sizeof(double2) + sizeof(int4) +
-                                                                        sizeof(int2))));
+  BL_CUDA(ctx, cudaMalloc(&s.span, (kQuadLevels + (s.span_cap + 1) + (size_t)kQuadLevels * s.span_cap + m) *
+                                        sizeof(int)));
+  BL_CUDA(ctx, cudaMalloc(&s.span_stage, (size_t)kTopCtas * kTopCap * (4 * sizeof(double2) + 2 * sizeof(int4))));
   BL_CUDA(ctx, cudaMalloc(&s.qcen, m * sizeof(double2)));
   BL_CUDA(ctx, cudaMalloc(&s.qbelow, m * sizeof(int)));
   BL_CUDA(ctx, cudaMalloc(&s.startcnt, (m + 1) * sizeof(int)));
@@ -1493,8 +1587,9 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
   radix_tree_kernel<<<nblk(n - 1, 256), 256, 0, st>>>(s.keys, n, s.bchild, s.brange, s.bdelta, s.bparent,
                                                        reinterpret_cast<int *>(s.bnode));
   bl_time_end(ctx, "gather_tree");
-  BL_CUDA(ctx, cudaMemsetAsync(s.span, 0, kQuadLevels * sizeof(int), st));
-  BL_CUDA(ctx, cudaMemsetAsync(s.startcnt + n, 0, sizeof(int), st));
+  const int ncb = nblk(n, kCenSpan);  // centroid blocks
+  // span_cnt and the block totals to 0
+  BL_CUDA(ctx, cudaMemsetAsync(s.span, 0, (kQuadLevels + ncb + 1) * sizeof(int), st));
   TreeArgs t;
   t.n = n;
   t.spos = s.spos;
@@ -1509,49 +1604,54 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
   t.qpar = s.qpar;
   t.qnchild = s.qnchild;
   t.span_cnt = s.span;
-  t.span_list = s.span + kQuadLevels;
+  t.blocktot = s.span + kQuadLevels;
+  t.span_list = t.blocktot + s.span_cap + 1;
   t.span_cap = s.span_cap;
-  t.span_pos = s.span + kQuadLevels + (size_t)kQuadLevels * s.span_cap;
+  t.span_pos = t.span_list + (size_t)kQuadLevels * s.span_cap;
+  t.startbase = s.startbase;
+  t.frame = s.frame;
+  t.inv_theta2 = 1.0 / (theta * theta);
+  t.nodes = s.nodes;
+  t.nodes_c64 = s.nodes_c64;
+  t.nodes_lvl = s.nodes_lvl;
   t.stage_val = reinterpret_cast<double2 *>(s.span_stage);
   t.stage_pend = reinterpret_cast<int4 *>(t.stage_val + 4 * kTopCtas * kTopCap);
-  t.stage_meta = reinterpret_cast<int2 *>(t.stage_pend + kTopCtas * kTopCap);
+  t.stage_meta = reinterpret_cast<int4 *>(t.stage_pend + kTopCtas * kTopCap);
   t.bnode = s.bnode;
   t.st = s.status;
   bl_time_begin(ctx, "chain_kernel");
   chain_kernel<<<nblk(n, 256), 256, 0, st>>>(t);
+  block_base_kernel<<<1, 1024, 0, st>>>(t.blocktot, ncb, s.startbase + n);
+  ctx->launches++;
   bl_time_end(ctx, "chain_kernel");
   bl_time_begin(ctx, "centroid_kernel");
   centroid_kernel<<<nblk(n, kCenSpan), kCenThreads, sizeof(CenSmem), st>>>(t);
+  // the points' and the local quad nodes' records on the side stream, beside
+  // the spanning nodes' cluster pass (which leaves all but a few SMs free);
+  // the cluster is enqueued first, so that it finds its SMs before the side
+  // kernel fills them
+  const bool fork = ctx->side && ctx->ev_fork && ctx->ev_join;
+  const bool spans = nblk(n, kCenSpan) > 1;  // one block has no spanning node
   bl_time_begin(ctx, "centroid_top");
-  if (nblk(n, kCenSpan) > 1) {  // one block has no spanning node
+  if (spans) {
     span_stage_kernel<<<kTopCtas * kTopCap / kStageThreads, kStageThreads, 0, st>>>(t);
+    ctx->launches++;
+  }
+  if (fork) BL_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
+  if (spans) {
     centroid_top_kernel<<<kTopCtas, kTopThreads, sizeof(TopSmem), st>>>(t);
-    ctx->launches += 2;
+    ctx->launches++;
+  }
+  if (fork) BL_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+  layout_local_kernel<<<nblk(n, 256), 256, 0, fork ? ctx->side : st>>>(t);
+  ctx->launches++;
+  if (fork) {
+    BL_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
+    BL_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
   }
   bl_time_end(ctx, "centroid_top");
   bl_time_end(ctx, "centroid_kernel");
   ctx->launches += 4;
-  bl_time_begin(ctx, "scan_layout");
-  if (int rc = scan_exclusive_int(ctx, s.startcnt, s.startbase, n + 1)) return rc;
-  LayoutArgs L;
-  L.n = n;
-  L.inv_theta2 = 1.0 / (theta * theta);
-  L.spos = s.spos;
-  L.range = s.brange;
-  L.dlt = s.bdelta;
-  L.parent = s.bparent;
-  L.qcen = s.qcen;
-  L.qbelow = s.qbelow;
-  L.startcnt = s.startcnt;
-  L.startbase = s.startbase;
-  L.frame = s.frame;
-  L.nodes = s.nodes;
-  L.nodes_c64 = s.nodes_c64;
-  L.nodes_lvl = s.nodes_lvl;
-  L.st = s.status;
-  layout_kernel<<<nblk(n, 256), 256, 0, st>>>(L, t);
-  bl_time_end(ctx, "scan_layout");
-  ctx->launches++;
   BL_CUDA(ctx, cudaGetLastError());
   return 0;
 }

@@ -216,7 +216,6 @@ struct Scratch {
   int *qbelow = nullptr;         // chain length below a quad node
   int *startcnt = nullptr;       // quad nodes starting at each sorted position (n+1)
   int *startbase = nullptr;      // exclusive scan of startcnt (n+1)
-  int *scan_tmp = nullptr;
   float4 *nodes = nullptr;       // pre-order records {x, y, D^2, skip}
   double2 *nodes_c64 = nullptr;  // FP64 centroid per pre-order record
   unsigned char *nodes_lvl = nullptr;
@@ -238,6 +237,10 @@ struct bl_ctx {
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
+  // a second stream for work beside the main one inside an iteration (forked
+  // from and joined back to `stream` by the two events)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::string err;
   // run options (reference constructor arguments)
   std::string input, outputdir, initfile;
@@ -312,5 +315,4 @@ int bh_graph_iterations(bl_ctx *ctx, int batch, double theta, double *step, int 
 int bh_graph_energy_iteration(bl_ctx *ctx, int batch, double theta, double step, double *energy_out);
 int bh_run(bl_ctx *ctx, int iterations, int batch, double theta, double *step, double *energy);
 int energy_reduce(bl_ctx *ctx, double *out_host);
-int scan_exclusive_int(bl_ctx *ctx, const int *in, int *out, int n);
 }  // namespace bl

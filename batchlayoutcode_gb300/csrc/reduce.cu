@@ -45,82 +45,6 @@ __global__ void __launch_bounds__(kRedThreads) energy_pass2(const double *__rest
   if (threadIdx.x == 0) out[0] = v;
 }
 
-constexpr int kScanThreads = 512;
-constexpr int kScanItems = 8;
-constexpr int kScanTile = kScanThreads * kScanItems;
-
-__device__ int block_exclusive_scan(int v, int *total) {
-  __shared__ int ws[kScanThreads / 32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int x = v;
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) ws[w] = x;
-  __syncthreads();
-  if (w == 0) {
-    int s = (lane < kScanThreads / 32) ? ws[lane] : 0;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, s, o);
-      if (lane >= o) s += y;
-    }
-    if (lane < kScanThreads / 32) ws[lane] = s;
-  }
-  __syncthreads();
-  const int before = (w > 0) ? ws[w - 1] : 0;
-  if (total) *total = ws[kScanThreads / 32 - 1];
-  return before + x - v;
-}
-
-// pass 1: per-tile exclusive scan in place + tile totals
-__global__ void __launch_bounds__(kScanThreads) scan_tiles(const int *__restrict__ in, int *out,
-                                                           int n, int *tile_tot) {
-  const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
-  int v[kScanItems];
-  int s = 0;
-#pragma unroll
-  for (int k = 0; k < kScanItems; k++) {
-    v[k] = (base + k < n) ? in[base + k] : 0;
-    s += v[k];
-  }
-  __shared__ int tot;
-  int run = block_exclusive_scan(s, &tot);
-#pragma unroll
-  for (int k = 0; k < kScanItems; k++) {
-    if (base + k < n) out[base + k] = run;
-    run += v[k];
-  }
-  if (threadIdx.x == 0) tile_tot[blockIdx.x] = tot;
-}
-
-// pass 2: scan of the tile totals (one block, looping over chunks)
-__global__ void __launch_bounds__(kScanThreads) scan_totals(int *tile_tot, int ntiles) {
-  __shared__ int carry;
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
-  for (int c0 = 0; c0 < ntiles; c0 += kScanThreads) {
-    const int i = c0 + threadIdx.x;
-    const int v = (i < ntiles) ? tile_tot[i] : 0;
-    __shared__ int tot;
-    const int ex = block_exclusive_scan(v, &tot);
-    const int base = carry;
-    __syncthreads();
-    if (i < ntiles) tile_tot[i] = base + ex;
-    __syncthreads();
-    if (threadIdx.x == 0) carry = base + tot;
-    __syncthreads();
-  }
-}
-
-__global__ void __launch_bounds__(kScanThreads) scan_add(int *out, int n, const int *tile_tot) {
-  const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanItems;
-  const int add = tile_tot[blockIdx.x];
-#pragma unroll
-  for (int k = 0; k < kScanItems; k++)
-    if (base + k < n) out[base + k] += add;
-}
-
 }  // namespace
 
 int energy_reduce(bl_ctx *ctx, double *out_host) {
@@ -133,18 +57,6 @@ int energy_reduce(bl_ctx *ctx, double *out_host) {
     BL_CUDA(ctx, cudaMemcpyAsync(out_host, ctx->s.energy, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     BL_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   }
-  return 0;
-}
-
-int scan_exclusive_int(bl_ctx *ctx, const int *in, int *out, int n) {
-  const int ntiles = (n + kScanTile - 1) / kScanTile;
-  if (!ctx->s.scan_tmp) BL_CUDA(ctx, cudaMalloc(&ctx->s.scan_tmp, sizeof(int) * 65536));
-  if (ntiles > 65536) return bl_fail(ctx, -5, "scan too large");
-  scan_tiles<<<ntiles, kScanThreads, 0, ctx->stream>>>(in, out, n, ctx->s.scan_tmp);
-  scan_totals<<<1, kScanThreads, 0, ctx->stream>>>(ctx->s.scan_tmp, ntiles);
-  scan_add<<<ntiles, kScanThreads, 0, ctx->stream>>>(out, n, ctx->s.scan_tmp);
-  ctx->launches += 3;
-  BL_CUDA(ctx, cudaGetLastError());
   return 0;
 }
 

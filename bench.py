@@ -627,7 +627,7 @@ def run_batched(args, w, ws, rank, local):
 # Labels the library times with CUDA events around each stage of a
 # Barnes-Hut iteration (direct launches, not the replayed graph).
 BH_STAGES = ["frame_morton", "lsd_passes", "radix_sort", "gather_tree", "chain_kernel", "centroid_top",
-             "centroid_kernel", "scan_layout", "traverse_kernel", "sweep_kernel"]
+             "centroid_kernel", "traverse_kernel", "sweep_kernel"]
 
 
 def stage_times(a, w, flush, steps, warmup):

@@ -664,7 +664,7 @@ def test_kernels_do_not_spill(L):
     reps = ptxas_reports()
     assert len(reps) >= 50
     for hot in ("traverse_kernel", "sweep_kernel", "centroid_kernel", "chain_kernel", "radix_tree_kernel",
-                "minibatch_kernel", "layout_kernel", "greedy_iteration_kernel"):
+                "minibatch_kernel", "centroid_top_kernel", "span_stage_kernel", "greedy_iteration_kernel"):
         assert any(hot in k for k in reps), hot
     bad = []
     for k, spill in reps.items():
