@@ -41,6 +41,8 @@
 namespace bl {
 namespace {
 
+constexpr int kQuadLevels = 33;  // quad levels 0..31, 32 for runs of identical keys
+
 
 // ---- stable LSD radix sort, 8-bit digits ------------------------------------
 //
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
 __global__ void __launch_bounds__(kRsThreads, 8) frame_keys_kernel(const float2 *__restrict__ pos, int n, int ntiles,
                                                                 unsigned int *box, double *frame, u64 *keys,
                                                                 int *vals, int shift, unsigned int *hist,
-                                                                DevStatus *st) {
+                                                                double inv_theta2, float *ztab, DevStatus *st) {
   __shared__ unsigned int s_box[kRsWarps][4];
   __shared__ unsigned int cnt[kRsWarps][256];
   __shared__ double s_frame[4];
@@ -292,6 +294,8 @@ __global__ void __launch_bounds__(kRsThreads, 8) frame_keys_kernel(const float2 
   __syncthreads();
   if (!s_ok) return;
   const double minX = s_frame[0], minY = s_frame[1], maxmin = s_frame[2], inv = s_frame[3];
+  // the records' z by quad level: D^2 / theta^2 with D = MAXMIN / 2^level
+  if (blockIdx.x == 0 && tid < kQuadLevels) ztab[tid] = bh_record_z(ldexp(maxmin, -tid), inv_theta2);
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
 #pragma unroll
     for (int w = 0; w < kRsWarps; w++) cnt[w][tid] = 0;
@@ -589,8 +593,7 @@ struct TreeArgs {
   // startbase[k] = quad nodes starting before sorted position k
   int *blocktot;
   int *startbase;
-  const double *frame;
-  double inv_theta2;  // 1 / theta^2, folded into the records' z
+  const float *ztab;  // the records' z = D^2 / theta^2 by quad level (frame_keys_kernel)
   float4 *nodes;
   double2 *nodes_c64;
   unsigned char *nodes_lvl;
@@ -748,8 +751,7 @@ __device__ __forceinline__ bool node_record_slot(const TreeArgs &t, int lo, int 
 // {x, y, D^2 / theta^2, skip} with the FP64 centroid and the level beside it
 // (the walk's FP64 re-test reads those two).
 __device__ __forceinline__ void write_node_record(const TreeArgs &t, int idx, int skip, int lvl, double2 c) {
-  const double D = ldexp(t.frame[2], -lvl);
-  t.nodes[idx] = make_float4(d2f_int(c.x), d2f_int(c.y), bh_record_z(D, t.inv_theta2), __int_as_float(skip));
+  t.nodes[idx] = make_float4(d2f_int(c.x), d2f_int(c.y), t.ztab[lvl], __int_as_float(skip));
   t.nodes_c64[idx] = c;
   t.nodes_lvl[idx] = (unsigned char)lvl;
 }
@@ -786,7 +788,6 @@ __device__ __forceinline__ void write_node_record_global(const TreeArgs &t, int 
 // than there are blocks.
 constexpr int kCenThreads = 512;
 constexpr int kCenSpan = kCenSpanC;
-constexpr int kQuadLevels = 33;  // quad levels 0..31, 32 for runs of identical keys
 
 struct CenSmem {
   double2 cen[kCenSpan];
@@ -1484,7 +1485,7 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   auto fr = [](void *p) { if (p) cudaFree(p); };
   fr(s.keys); fr(s.keys_alt); fr(s.perm); fr(s.perm_alt); fr(s.hist); fr(s.spos);
   fr(s.bparent); fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.qkids); fr(s.qpar); fr(s.qnchild);
-  fr(s.span); fr(s.span_stage); fr(s.qcen);
+  fr(s.span); fr(s.span_stage); fr(s.ztab); fr(s.qcen);
   fr(s.qbelow); fr(s.startcnt); fr(s.startbase); fr(s.nodes); fr(s.nodes_c64);
   fr(s.nodes_lvl); fr(s.rep); fr(s.f0); fr(s.pos_alt); fr(s.runs); fr(s.bnode);
   const size_t nb = (n + kRsTile - 1) / kRsTile;
@@ -1504,6 +1505,7 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   BL_CUDA(ctx, cudaMalloc(&s.qkids, m * sizeof(int4)));
   BL_CUDA(ctx, cudaMalloc(&s.qpar, 2 * m * sizeof(int)));
   BL_CUDA(ctx, cudaMalloc(&s.qnchild, m * sizeof(int)));
+  BL_CUDA(ctx, cudaMalloc(&s.ztab, kQuadLevels * sizeof(float)));
   s.span_cap = nblk((long long)m, kCenSpan);
   BL_CUDA(ctx, cudaMalloc(&s.span, (kQuadLevels + (s.span_cap + 1) + (size_t)kQuadLevels * s.span_cap + m) *
                                         sizeof(int)));
@@ -1555,7 +1557,9 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
     int shift = 32;
     int nn = n;
     int ntiles = nb;
-    void *args[] = {(void *)&pos, &nn, &ntiles, &s.bbox, &s.frame, &s.keys, &s.perm, &shift, &s.hist, &s.status};
+    double inv_theta2 = 1.0 / (theta * theta);
+    void *args[] = {(void *)&pos, &nn, &ntiles, &s.bbox, &s.frame, &s.keys, &s.perm, &shift, &s.hist,
+                    &inv_theta2, &s.ztab, &s.status};
     BL_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)frame_keys_kernel, dim3(grid), dim3(kRsThreads), args, 0,
                                              st));
     ctx->launches++;
@@ -1609,8 +1613,7 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
   t.span_cap = s.span_cap;
   t.span_pos = t.span_list + (size_t)kQuadLevels * s.span_cap;
   t.startbase = s.startbase;
-  t.frame = s.frame;
-  t.inv_theta2 = 1.0 / (theta * theta);
+  t.ztab = s.ztab;
   t.nodes = s.nodes;
   t.nodes_c64 = s.nodes_c64;
   t.nodes_lvl = s.nodes_lvl;

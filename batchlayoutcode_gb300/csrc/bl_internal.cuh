@@ -212,6 +212,7 @@ struct Scratch {
   int *span = nullptr;           // centroid pass: spanning quad nodes per level (counts, then lists)
   int span_cap = 0;              // list slots per level (centroid blocks)
   void *span_stage = nullptr;    // staged spanning nodes for the cluster pass
+  float *ztab = nullptr;         // pre-order records' z by quad level
   double2 *qcen = nullptr;       // centroid of quad node (indexed by binary internal id)
   int *qbelow = nullptr;         // chain length below a quad node
   int *startcnt = nullptr;       // quad nodes starting at each sorted position (n+1)
