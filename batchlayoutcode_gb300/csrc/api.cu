@@ -172,7 +172,7 @@ void free_ctx(bl_ctx *c) {
   bl::Scratch &s = c->s;
   fr(s.energy_parts); fr(s.energy); fr(s.status); fr(s.partials); fr(s.keys); fr(s.keys_alt);
   fr(s.perm); fr(s.perm_alt); fr(s.hist); fr(s.bbox); fr(s.frame); fr(s.spos); fr(s.bparent);
-  fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.qkids); fr(s.qpar); fr(s.qnchild); fr(s.span); fr(s.span_stage); fr(s.ztab); fr(s.qcen); fr(s.qbelow); fr(s.startcnt);
+  fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.qkids); fr(s.qpar); fr(s.qnchild); fr(s.span); fr(s.span_stage); fr(s.ztab); fr(s.chain); fr(s.qcen); fr(s.qbelow); fr(s.startcnt);
   fr(s.startbase); fr(s.nodes); fr(s.nodes_c64); fr(s.nodes_lvl); fr(s.rep);
   fr(s.stats); fr(s.pos_alt); fr(s.f0); fr(s.runs); fr(s.bnode); fr(s.cursor); fr(s.cursor_full); fr(s.walk_off); fr(s.walk_pairs);
   fr(s.term_off); fr(s.terms); fr(s.term_tgt); fr(s.greedy_share); fr(s.greedy_pos);

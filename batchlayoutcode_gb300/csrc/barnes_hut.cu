@@ -593,6 +593,11 @@ struct TreeArgs {
   // startbase[k] = quad nodes starting before sorted position k
   int *blocktot;
   int *startbase;
+  // quad nodes that span exactly one block boundary, by boundary b (between
+  // blocks b and b+1): their levels (bit mask) and ids (chain_node[b * 33 +
+  // level])
+  unsigned long long *chain_mask;
+  int *chain_node;
   const float *ztab;  // the records' z = D^2 / theta^2 by quad level (frame_keys_kernel)
   float4 *nodes;
   double2 *nodes_c64;
@@ -846,6 +851,99 @@ __device__ double2 quad_centroid_global(const TreeArgs &t, int node) {
   return make_double2(div_count_int(cx, cnt), div_count_int(cy, cnt));
 }
 
+// Centroids of the quad nodes that contain boundary b and no other (one
+// warp).  They are nested, one per level, each the parent of the
+// next deeper one; their other children lie inside block b or b+1 (done) or
+// are points.  Lane i takes the i-th deepest node: its structure and its done
+// children are loaded in parallel, then the nodes are summed from the deepest
+// up, each taking the one below from the lane before it.
+__device__ __forceinline__ void chain_centroids(const TreeArgs &t, int b) {
+  const int lane = threadIdx.x & 31;
+  const unsigned long long mask = __ldcg(&t.chain_mask[b]);
+  const int cnt = __popcll(mask);
+  if (cnt == 0) return;
+  if (cnt > 32) {  // every level: one lane, in order (the others wait at the shuffle-free path)
+    if (lane == 0)
+      for (int lvl = kQuadLevels - 1; lvl >= 0; lvl--)
+        if ((mask >> lvl) & 1ull) {
+          const int node = __ldcg(&t.chain_node[b * kQuadLevels + lvl]);
+          t.qcen[node] = quad_centroid_global(t, node);
+        }
+    __syncwarp();
+    return;
+  }
+  // lane i: the level of the (i+1)-th highest set bit
+  int lvl = -1;
+  {
+    int seen = 0;
+    for (int l = kQuadLevels - 1; l >= 0; l--)
+      if ((mask >> l) & 1ull) {
+        if (seen == lane) lvl = l;
+        seen++;
+      }
+  }
+  const bool mine = lane < cnt;
+  const int node = mine ? __ldcg(&t.chain_node[b * kQuadLevels + lvl]) : -1;
+  const int below = __shfl_up_sync(0xffffffffu, node, 1);  // the next deeper chain node
+  double2 v[4] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+  int nc = 0, from_below = -1;
+  double2 run = make_double2(0.0, 0.0);
+  bool is_run = false;
+  if (mine) {
+    const int p = t.dlt[node];
+    if (p >= 64) {  // a run: points only
+      is_run = true;
+      run = quad_centroid_global(t, node);
+    } else {
+      const int4 kk = t.qkids[node];
+      const int kids[4] = {kk.x, kk.y, kk.z, kk.w};
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const int ch = kids[c];
+        if (ch == kNoChild) continue;
+        nc = c + 1;
+        if (lane > 0 && ch == below) {
+          from_below = c;
+        } else if (ch < 0) {
+          const float2 pt = t.spos[~ch];
+          v[c] = make_double2(f2d_int(pt.x), f2d_int(pt.y));
+        } else {
+          v[c] = __ldcg(&t.qcen[ch]);
+        }
+      }
+    }
+  }
+  double2 prev = make_double2(0.0, 0.0), mine_c = make_double2(0.0, 0.0);
+  for (int i = 0; i < cnt; i++) {
+    if (lane == i) {
+      if (is_run) {
+        mine_c = run;
+      } else {
+        double cx = 0.0, cy = 0.0;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          if (c >= nc) break;
+          const double2 u = c == from_below ? prev : v[c];
+          cx = c ? __dadd_rn(cx, u.x) : zero_plus(u.x);
+          cy = c ? __dadd_rn(cy, u.y) : zero_plus(u.y);
+        }
+        mine_c = make_double2(div_count_int(cx, nc), div_count_int(cy, nc));
+      }
+    }
+    prev.x = __shfl_sync(0xffffffffu, mine_c.x, i);
+    prev.y = __shfl_sync(0xffffffffu, mine_c.y, i);
+  }
+  if (mine) t.qcen[node] = mine_c;
+}
+
+// One warp per block boundary (boundaries 0 .. nb-2).
+constexpr int kChainThreads = 128;
+__global__ void __launch_bounds__(kChainThreads) boundary_chain_kernel(TreeArgs t, int nbound) {
+  if (!block_status_ok(t.st)) return;
+  const int b = blockIdx.x * (kChainThreads / 32) + (threadIdx.x >> 5);
+  if (b < nbound) chain_centroids(t, b);
+}
+
 __global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   CenSmem &S = *reinterpret_cast<CenSmem *>(smem_raw);
@@ -867,11 +965,17 @@ __global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
         S.kids[q] = t.qkids[j];
         S.dlt[q] = t.dlt[j];
         S.par[q] = t.qpar[j];
-      } else if (m > 0) {  // spans blocks: computed by centroid_top_kernel
+      } else if (m > 0) {  // spans blocks
         const int lvl = quad_level(t.dlt[j]);
-        const int slot = atomicAdd(&t.span_cnt[lvl], 1);
-        if (slot < t.span_cap) t.span_list[lvl * t.span_cap + slot] = j;
-        else dev_record_error(t.st, DEV_BAD_INDEX);  // cannot happen (see above)
+        const int bl = rg.x / kCenSpan;
+        if (rg.y / kCenSpan == bl + 1) {  // one boundary: boundary_chain_kernel
+          t.chain_node[bl * kQuadLevels + lvl] = j;
+          atomicOr(&t.chain_mask[bl], 1ull << lvl);
+        } else {  // more: centroid_top_kernel
+          const int slot = atomicAdd(&t.span_cnt[lvl], 1);
+          if (slot < t.span_cap) t.span_list[lvl * t.span_cap + slot] = j;
+          else dev_record_error(t.st, DEV_BAD_INDEX);  // cannot happen (see above)
+        }
       }
     }
     S.need[q] = (unsigned short)need;
@@ -966,29 +1070,42 @@ __global__ void __launch_bounds__(kCenThreads) centroid_kernel(TreeArgs t) {
 
 // Pre-order records of the points and of the quad nodes inside one centroid
 // block, one thread per sorted position (the nodes that span blocks are
-// written by centroid_top_kernel).  It runs beside the spanning nodes' pass.
+// written by boundary_chain_kernel and centroid_top_kernel, beside which this
+// kernel runs).
 __global__ void __launch_bounds__(256) layout_local_kernel(TreeArgs t) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (!block_status_ok(t.st)) return;
   const int cap = 2 * t.n - 1;  // records: n leaves + at most n-1 quad nodes
-  if (i < t.n) {  // leaf (sorted point) i
-    const int idx = i + t.startbase[i] + t.startcnt[i];
+  // every load that depends only on i first, then the range ends' offsets
+  const bool leaf = i < t.n, inner = i < t.n - 1;
+  const int sb = leaf ? t.startbase[i] : 0, sc = leaf ? t.startcnt[i] : 0;
+  const float2 pt = leaf ? t.spos[i] : make_float2(0.f, 0.f);
+  const int m = inner ? t.qnchild[i] : 0;
+  const int2 rg = inner ? t.range[i] : make_int2(0, 0);
+  const int qb = inner ? t.qbelow[i] : 0;
+  const int p = inner ? t.dlt[i] : 0;
+  const double2 c = inner ? t.qcen[i] : make_double2(0.0, 0.0);
+  // a quad node (binary internal node i) inside one block or spanning one
+  // boundary; the nodes spanning more are written by centroid_top_kernel
+  const bool node = m > 0 && rg.y / kCenSpan - rg.x / kCenSpan <= 1;
+  int sc_lo = 0, sb_lo = 0, sb_hi = 0;
+  if (node) {
+    sc_lo = t.startcnt[rg.x];
+    sb_lo = t.startbase[rg.x];
+    sb_hi = t.startbase[rg.y + 1];
+  }
+  if (leaf) {  // leaf (sorted point) i, after the quad nodes starting at i
+    const int idx = i + sb + sc;
     if (idx < 0 || idx >= cap) {
       dev_record_error(t.st, DEV_BAD_INDEX);
       return;
     }
-    const float2 p = t.spos[i];
     // a leaf's z = -inf is never in doubt: no FP64 centroid or level needed
-    t.nodes[idx] = make_float4(p.x, p.y, kLeafZ, __int_as_float(idx + 1));
+    t.nodes[idx] = make_float4(pt.x, pt.y, kLeafZ, __int_as_float(idx + 1));
   }
-  if (i < t.n - 1 && t.qnchild[i] > 0) {  // a quad node (binary internal node i)
-    const int2 rg = t.range[i];
-    if (rg.x / kCenSpan != rg.y / kCenSpan) return;  // spans blocks
-    int idx, skip;
-    if (node_record_slot(t, rg.x, rg.y + 1, t.qbelow[i], t.startcnt[rg.x], t.startbase[rg.x],
-                         t.startbase[rg.y + 1], idx, skip))
-      write_node_record(t, idx, skip, quad_level(t.dlt[i]), t.qcen[i]);
-  }
+  int idx, skip;
+  if (node && node_record_slot(t, rg.x, rg.y + 1, qb, sc_lo, sb_lo, sb_hi, idx, skip))
+    write_node_record(t, idx, skip, quad_level(p), c);
 }
 
 constexpr int kTopCtas = 8;  // one cluster (the portable maximum size)
@@ -1100,7 +1217,7 @@ __global__ void __launch_bounds__(kStageThreads) span_stage_kernel(TreeArgs t) {
       pt[c] = t.spos[~ch];
     } else {
       rg[c] = t.range[ch];
-      qc[c] = __ldcg(&t.qcen[ch]);  // used only when the child is inside one block
+      qc[c] = __ldcg(&t.qcen[ch]);  // used only when the child is done (at most one boundary)
     }
   }
   int pend[4] = {-1, -1, -1, -1};
@@ -1112,7 +1229,7 @@ __global__ void __launch_bounds__(kStageThreads) span_stage_kernel(TreeArgs t) {
     nc++;
     double2 v = make_double2(0.0, 0.0);
     if (ch < 0) v = make_double2(f2d_int(pt[c].x), f2d_int(pt[c].y));
-    else if (rg[c].x / kCenSpan != rg[c].y / kCenSpan) pend[c] = ch;  // listed
+    else if (rg[c].y / kCenSpan - rg[c].x / kCenSpan >= 2) pend[c] = ch;  // listed
     else v = qc[c];
     t.stage_val[(size_t)c * kTopCtas * kTopCap + idx] = v;
   }
@@ -1485,7 +1602,7 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   auto fr = [](void *p) { if (p) cudaFree(p); };
   fr(s.keys); fr(s.keys_alt); fr(s.perm); fr(s.perm_alt); fr(s.hist); fr(s.spos);
   fr(s.bparent); fr(s.bchild); fr(s.brange); fr(s.bdelta); fr(s.qkids); fr(s.qpar); fr(s.qnchild);
-  fr(s.span); fr(s.span_stage); fr(s.ztab); fr(s.qcen);
+  fr(s.span); fr(s.span_stage); fr(s.ztab); fr(s.chain); fr(s.qcen);
   fr(s.qbelow); fr(s.startcnt); fr(s.startbase); fr(s.nodes); fr(s.nodes_c64);
   fr(s.nodes_lvl); fr(s.rep); fr(s.f0); fr(s.pos_alt); fr(s.runs); fr(s.bnode);
   const size_t nb = (n + kRsTile - 1) / kRsTile;
@@ -1506,6 +1623,10 @@ int ensure_bh_scratch(bl_ctx *ctx) {
   BL_CUDA(ctx, cudaMalloc(&s.qpar, 2 * m * sizeof(int)));
   BL_CUDA(ctx, cudaMalloc(&s.qnchild, m * sizeof(int)));
   BL_CUDA(ctx, cudaMalloc(&s.ztab, kQuadLevels * sizeof(float)));
+  {
+    const size_t cap = (size_t)nblk((long long)m, kCenSpan);
+    BL_CUDA(ctx, cudaMalloc(&s.chain, cap * (sizeof(unsigned long long) + kQuadLevels * sizeof(int))));
+  }
   s.span_cap = nblk((long long)m, kCenSpan);
   BL_CUDA(ctx, cudaMalloc(&s.span, (kQuadLevels + (s.span_cap + 1) + (size_t)kQuadLevels * s.span_cap + m) *
                                         sizeof(int)));
@@ -1592,8 +1713,9 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
                                                        reinterpret_cast<int *>(s.bnode));
   bl_time_end(ctx, "gather_tree");
   const int ncb = nblk(n, kCenSpan);  // centroid blocks
-  // span_cnt and the block totals to 0
+  // span_cnt, the block totals and the boundary chains' level masks to 0
   BL_CUDA(ctx, cudaMemsetAsync(s.span, 0, (kQuadLevels + ncb + 1) * sizeof(int), st));
+  BL_CUDA(ctx, cudaMemsetAsync(s.chain, 0, (size_t)ncb * sizeof(unsigned long long), st));
   TreeArgs t;
   t.n = n;
   t.spos = s.spos;
@@ -1614,6 +1736,8 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
   t.span_pos = t.span_list + (size_t)kQuadLevels * s.span_cap;
   t.startbase = s.startbase;
   t.ztab = s.ztab;
+  t.chain_mask = reinterpret_cast<unsigned long long *>(s.chain);
+  t.chain_node = reinterpret_cast<int *>(t.chain_mask + s.span_cap);
   t.nodes = s.nodes;
   t.nodes_c64 = s.nodes_c64;
   t.nodes_lvl = s.nodes_lvl;
@@ -1629,29 +1753,30 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
   bl_time_end(ctx, "chain_kernel");
   bl_time_begin(ctx, "centroid_kernel");
   centroid_kernel<<<nblk(n, kCenSpan), kCenThreads, sizeof(CenSmem), st>>>(t);
-  // the points' and the local quad nodes' records on the side stream, beside
-  // the spanning nodes' cluster pass (which leaves all but a few SMs free);
-  // the cluster is enqueued first, so that it finds its SMs before the side
-  // kernel fills them
+  // the quad nodes spanning one boundary (one warp per boundary); then the
+  // records of the points and of the nodes spanning at most one boundary on
+  // the side stream (at the lower priority), beside the nodes spanning more
+  // (one cluster, which leaves most SMs free)
   const bool fork = ctx->side && ctx->ev_fork && ctx->ev_join;
-  const bool spans = nblk(n, kCenSpan) > 1;  // one block has no spanning node
+  const bool spans = ncb > 1;  // one block has no spanning node
   bl_time_begin(ctx, "centroid_top");
   if (spans) {
-    span_stage_kernel<<<kTopCtas * kTopCap / kStageThreads, kStageThreads, 0, st>>>(t);
+    boundary_chain_kernel<<<nblk(ncb - 1, kChainThreads / 32), kChainThreads, 0, st>>>(t, ncb - 1);
     ctx->launches++;
   }
-  if (fork) BL_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
-  if (spans) {
-    centroid_top_kernel<<<kTopCtas, kTopThreads, sizeof(TopSmem), st>>>(t);
-    ctx->launches++;
+  if (fork) {
+    BL_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
+    BL_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
   }
-  if (fork) BL_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
   layout_local_kernel<<<nblk(n, 256), 256, 0, fork ? ctx->side : st>>>(t);
   ctx->launches++;
-  if (fork) {
-    BL_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
-    BL_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
+  if (fork) BL_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
+  if (spans) {
+    span_stage_kernel<<<kTopCtas * kTopCap / kStageThreads, kStageThreads, 0, st>>>(t);
+    centroid_top_kernel<<<kTopCtas, kTopThreads, sizeof(TopSmem), st>>>(t);
+    ctx->launches += 2;
   }
+  if (fork) BL_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
   bl_time_end(ctx, "centroid_top");
   bl_time_end(ctx, "centroid_kernel");
   ctx->launches += 4;

@@ -213,6 +213,7 @@ struct Scratch {
   int span_cap = 0;              // list slots per level (centroid blocks)
   void *span_stage = nullptr;    // staged spanning nodes for the cluster pass
   float *ztab = nullptr;         // pre-order records' z by quad level
+  void *chain = nullptr;         // centroid pass: nodes spanning one block boundary, per boundary
   double2 *qcen = nullptr;       // centroid of quad node (indexed by binary internal id)
   int *qbelow = nullptr;         // chain length below a quad node
   int *startcnt = nullptr;       // quad nodes starting at each sorted position (n+1)

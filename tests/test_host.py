@@ -648,7 +648,8 @@ def ptxas_reports():
         path = os.path.join(ROOT, "batchlayoutcode_gb300", "_build", src + ".ptxas.txt")
         cur = None
         for line in open(path).read().splitlines():
-            m = re.search(r"Compiling entry function '([^']+)'", line)
+            # a report belongs to the entry or device function it follows
+            m = re.search(r"(?:Compiling entry function|Function properties for) '?([A-Za-z0-9_]+)'?", line)
             if m:
                 cur = m.group(1)
             m = re.search(r"(\d+) bytes spill stores, (\d+) bytes spill loads", line)
@@ -664,7 +665,8 @@ def test_kernels_do_not_spill(L):
     reps = ptxas_reports()
     assert len(reps) >= 50
     for hot in ("traverse_kernel", "sweep_kernel", "centroid_kernel", "chain_kernel", "radix_tree_kernel",
-                "minibatch_kernel", "centroid_top_kernel", "span_stage_kernel", "greedy_iteration_kernel"):
+                "minibatch_kernel", "centroid_top_kernel", "span_stage_kernel", "boundary_chain_kernel",
+                "layout_local_kernel", "greedy_iteration_kernel"):
         assert any(hot in k for k in reps), hot
     bad = []
     for k, spill in reps.items():
