@@ -770,27 +770,32 @@ __device__ __forceinline__ void write_node_record_global(const TreeArgs &t, int 
     write_node_record(t, idx, skip, quad_level(t.dlt[node]), c);
 }
 
-// Centroids bottom-up in two launches.  The centroid of a quad node is the
-// unweighted mean of its children summed in quadrant order in FP64
-// (BarnesHut.h:197-217), bit-identical to the reference; it can be computed
-// once every child is done.  centroid_kernel: a block owns kCenSpan
-// consecutive sorted points; a binary node whose range lies inside them has
-// its index there too (a Karras node's index is one of its range ends), so
-// the block loads those nodes' structure and its points into shared memory
-// with coalesced reads, and processes the nodes in rounds: the nodes whose
-// children are all done form a queue, handled one node per thread so that the
-// FP64 work (a small fraction of the FP32 rate on this part, charged per warp
-// instruction) runs in full warps, and a node's last arriving child appends
-// it to the next round's queue.  A quad node whose range spans blocks is only
-// listed, by level.  span_stage_kernel gathers the listed nodes' children
-// over the whole device; centroid_top_kernel, one thread-block cluster,
-// computes the listed nodes level by level from the deepest, a cluster
-// barrier between levels — a node's children are one level deeper at least,
-// so each level finds its children done.  (This replaced a climb by the last
-// arriving child through device-scope counters: one serial chain of L2 round
-// trips per level, 58 us of the pass on a 1M-point tree against 40 us now.)  At one level the quad nodes' ranges are disjoint
-// and a spanning one contains a block boundary, so a level lists fewer nodes
-// than there are blocks.
+// Centroids bottom-up.  The centroid of a quad node is the unweighted mean of
+// its children summed in quadrant order in FP64 (BarnesHut.h:197-217),
+// bit-identical to the reference; it can be computed once every child is
+// done.  Three passes by how many block boundaries a node's range contains:
+// * none — centroid_kernel: a block owns kCenSpan consecutive sorted points;
+//   a binary node whose range lies inside them has its index there too (a
+//   Karras node's index is one of its range ends), so the block loads those
+//   nodes' structure and its points into shared memory with coalesced reads,
+//   and processes the nodes in rounds: the nodes whose children are all done
+//   form a queue, handled one node per thread so that the FP64 work (a small
+//   fraction of the FP32 rate on this part, charged per warp instruction)
+//   runs in full warps, and a node's last arriving child appends it to the
+//   next round's queue.  The block also lists the spanning nodes whose index
+//   it holds.
+// * one — boundary_chain_kernel: the nodes containing boundary b and no other
+//   are nested, one per level; one warp computes them from the deepest up.
+// * more — span_stage_kernel gathers their children over the whole device;
+//   centroid_top_kernel, one thread-block cluster, computes them level by
+//   level from the deepest, a cluster barrier between levels (a node's
+//   children are one level deeper at least).  At one level the quad nodes'
+//   ranges are disjoint and each of these contains a block boundary, so a
+//   level lists fewer nodes than there are blocks.
+// On a uniform 1M-point tree ~5,200 nodes span blocks (15 levels), 341 of
+// them (5 levels) more than one boundary.  (A climb by the last arriving child
+// through device-scope counters did the spanning nodes before: one serial
+// chain of L2 round trips per level, 58 us of the pass.)
 constexpr int kCenThreads = 512;
 constexpr int kCenSpan = kCenSpanC;
 
