@@ -1117,7 +1117,7 @@ __global__ void __launch_bounds__(256) layout_local_kernel(TreeArgs t) {
 
 constexpr int kTopCtas = 8;  // one cluster (the portable maximum size)
 constexpr int kTopThreads = 1024;
-constexpr int kTopCap = 2048;  // listed nodes per block held in shared memory
+constexpr int kTopCap = 1024;  // listed nodes per block held in shared memory (104 KB)
 constexpr int kStageThreads = 128;
 
 __device__ __forceinline__ void top_cluster_sync() {

@@ -377,6 +377,31 @@ def test_rgg1m_traversal_decisions_exact(B, rgg1m, theta):
     assert rel_l2(rep, orep) <= FORCE_TOL
 
 
+def test_deep_tree_over_many_block_boundaries(B):
+    """10M points on the line y = x: every quad cell splits in two, so the
+    tree is binary and deep; ~9,750 of its nodes span two or more centroid
+    blocks (more than the cluster pass keeps in shared memory, so its levels
+    run through global memory) and ~90,000 span one (chains of up to ~18
+    levels per boundary).  Structure, every FP64 centroid, every opening
+    decision and the repulsion against the oracle."""
+    n = 10_000_000
+    rng = np.random.default_rng(3)
+    u = rng.uniform(-3.0, 3.0, n).astype(np.float32).astype(np.float64)
+    xy = np.stack([u, u], axis=1)
+    rowptr = np.zeros(n + 1, np.int32)
+    colids = np.zeros(0, np.int32)
+    with B.Algorithms(rowptr, colids) as a:
+        a.nCoordinates = xy
+        t = a.quadtree()
+        rep, (visits, _) = a.bh_repulsion(1.2)
+    ot = oracle.bh_tree(xy)
+    for k in ("lo", "hi", "depth", "nchild", "centroid"):
+        assert np.array_equal(t[k], ot[k]), k
+    orep, ovis = oracle.bh_repulsion(xy, xy, 1.2, visits=True)
+    assert visits == int(ovis.sum())
+    assert rel_l2(rep, orep) <= FORCE_TOL
+
+
 def test_chunglu100k_minibatch_iteration_forces(B):
     from batchlayoutcode_gb300 import graphs as G
     g, xy = G.cached_workload("chunglu100k")
