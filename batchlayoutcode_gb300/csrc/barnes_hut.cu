@@ -571,7 +571,6 @@ __global__ void radix_tree_kernel(const u64 *__restrict__ K, int n, int2 *child,
 struct TreeArgs {
   int n;
   const float2 *spos;
-  const int2 *child;
   const int2 *range;
   const int *dlt;
   const int *parent;
@@ -1726,7 +1725,6 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
   TreeArgs t;
   t.n = n;
   t.spos = s.spos;
-  t.child = s.bchild;
   t.range = s.brange;
   t.dlt = s.bdelta;
   t.parent = s.bparent;
