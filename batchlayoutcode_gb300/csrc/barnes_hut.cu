@@ -1368,15 +1368,23 @@ struct TraverseArgs {
   float2 *rep;
   double theta;
   unsigned long long *stats;  // [visits, fp64 decisions] or null
-  // attraction of neighbours that have not moved yet in this iteration
-  // (same or later batch), summed with the repulsion into f0; null to skip
+  // the attraction of the neighbours that have not moved yet in this
+  // iteration (unmoved_attraction_kernel); the walk adds minus the
+  // repulsion; null to skip
   float4 *f0;
-  const int *rowptr;
-  const int *colids;
-  const float2 *pold;
-  int batch;
-  float W;
 };
+
+// FR attraction (algorithms.cpp:1056-1058) of the neighbours of v that have
+// not moved before v in the iteration (same or later batch), float-float, by
+// vertex id.  It needs no tree, so it runs on the second stream beside the
+// tree's spanning passes; the walk then adds minus the repulsion.
+__global__ void __launch_bounds__(256) unmoved_attraction_kernel(int n, const int *__restrict__ rowptr,
+                                                                 const int *__restrict__ colids,
+                                                                 const float2 *pold, int batch, float W,
+                                                                 float4 *f0) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n) f0[v] = bh_unmoved_attraction(v, make_float2(0.f, 0.f), rowptr, colids, pold, batch, W);
+}
 
 
 // 128 threads per block: measured 1.5 % faster than 256 and 512 on the 1M
@@ -1400,9 +1408,13 @@ __global__ void __launch_bounds__(kTravThreads) traverse_kernel(TraverseArgs a) 
                                                 total, q, visits, exact);
   const int v = a.perm[k];
   a.rep[v] = rep;
-  // FR attraction (algorithms.cpp:1056-1058) of the neighbours that have not
-  // moved before v in this iteration
-  if (a.f0) a.f0[v] = bh_unmoved_attraction(v, rep, a.rowptr, a.colids, a.pold, a.batch, a.W);
+  // minus the repulsion into v's sum of unmoved neighbours' attraction
+  if (a.f0) {
+    float4 f = a.f0[v];  // {hx, hy, lx, ly}
+    ff_add(f.x, f.z, -rep.x);
+    ff_add(f.y, f.w, -rep.y);
+    a.f0[v] = f;
+  }
   if (kStats) {  // one atomic per group of converged lanes, not per thread
     const unsigned int m = __activemask();
     const unsigned int sv = __reduce_add_sync(m, visits), se = __reduce_add_sync(m, exact);
@@ -1665,7 +1677,7 @@ int ensure_bh_scratch(bl_ctx *ctx) {
 // Steps 1-4 for the positions `pos`; leaves the pre-order records in
 // ctx->s.nodes (total = n + number of quad nodes, read back by callers that
 // need it via startbase[n]).
-int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
+int bh_build(bl_ctx *ctx, const float2 *pos, double theta, int attract_batch) {
   const int n = ctx->g.n;
   Scratch &s = ctx->s;
   cudaStream_t st = ctx->stream;
@@ -1758,10 +1770,12 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
   bl_time_end(ctx, "chain_kernel");
   bl_time_begin(ctx, "centroid_kernel");
   centroid_kernel<<<nblk(n, kCenSpan), kCenThreads, sizeof(CenSmem), st>>>(t);
-  // the quad nodes spanning one boundary (one warp per boundary); then the
-  // records of the points and of the nodes spanning at most one boundary on
-  // the side stream (at the lower priority), beside the nodes spanning more
-  // (one cluster, which leaves most SMs free)
+  // the quad nodes spanning one boundary (one warp per boundary); then on the
+  // side stream (at the lower priority) the walk's attraction part and the
+  // records of the points and of the nodes spanning at most one boundary,
+  // beside the nodes spanning more (one cluster, which leaves most SMs free).
+  // (Started with the frame kernel instead, the attraction slowed that
+  // cooperative launch by more than it saved.)
   const bool fork = ctx->side && ctx->ev_fork && ctx->ev_join;
   const bool spans = ncb > 1;  // one block has no spanning node
   bl_time_begin(ctx, "centroid_top");
@@ -1772,6 +1786,11 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta) {
   if (fork) {
     BL_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
     BL_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+  }
+  if (attract_batch > 0) {  // the walk's attraction part (needs no tree), for the iteration that follows
+    unmoved_attraction_kernel<<<nblk(n, 256), 256, 0, fork ? ctx->side : st>>>(
+        n, ctx->g.rowptr, ctx->g.colids, pos, attract_batch, (float)ctx->weight, s.f0);
+    ctx->launches++;
   }
   layout_local_kernel<<<nblk(n, 256), 256, 0, fork ? ctx->side : st>>>(t);
   ctx->launches++;
@@ -1810,11 +1829,6 @@ int bh_traverse(bl_ctx *ctx, double theta, bool want_stats, int batch) {
   a.stats = want_stats ? s.stats : nullptr;
   a.st = s.status;
   a.f0 = batch > 0 ? s.f0 : nullptr;
-  a.rowptr = ctx->g.rowptr;
-  a.colids = ctx->g.colids;
-  a.pold = ctx->pos;
-  a.batch = batch > 0 ? batch : 1;
-  a.W = (float)ctx->weight;
   if (want_stats) BL_CUDA(ctx, cudaMemsetAsync(s.stats, 0, 2 * sizeof(unsigned long long), ctx->stream));
   bl_time_begin(ctx, "traverse_kernel");
   if (want_stats) traverse_kernel<true><<<nblk(n, kTravThreads), kTravThreads, 0, ctx->stream>>>(a);
@@ -1831,7 +1845,7 @@ int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_en
   const LevelSchedule *ls = level_schedule(ctx, batch);
   if (!ls) return -2;
   float2 *pold = ctx->pos, *pnew = ctx->s.pos_alt;
-  if (int rc = bh_build(ctx, pold, theta)) return rc;
+  if (int rc = bh_build(ctx, pold, theta, batch)) return rc;  // with the unmoved neighbours' attraction
   if (int rc = bh_traverse(ctx, theta, false, batch)) return rc;
   SweepArgs a;
   a.order = ls->order;

@@ -300,7 +300,10 @@ int greedy_walks_build(bl_ctx *ctx);
 int greedy_walk_run(bl_ctx *ctx, int batch, int iterations, double step0, double decay, bool want_energy,
                     double *energy_out);
 int ensure_bh_scratch(bl_ctx *ctx);
-int bh_build(bl_ctx *ctx, const float2 *pos, double theta);  // theta: folded into the walk records
+// theta: folded into the walk records; attract_batch > 0: also the
+// attraction of the neighbours not yet moved in an iteration with that batch
+// size into the force sums (bh_traverse with the same batch adds the rest)
+int bh_build(bl_ctx *ctx, const float2 *pos, double theta, int attract_batch = 0);
 int bh_traverse(bl_ctx *ctx, double theta, bool want_stats, int batch);
 int bh_iteration(bl_ctx *ctx, int batch, double theta, double step, bool want_energy,
                  double *energy_out);
