@@ -1383,7 +1383,7 @@ __global__ void __launch_bounds__(256) unmoved_attraction_kernel(int n, const in
                                                                  const float2 *pold, int batch, float W,
                                                                  float4 *f0) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v < n) f0[v] = bh_unmoved_attraction(v, make_float2(0.f, 0.f), rowptr, colids, pold, batch, W);
+  if (v < n) f0[v] = bh_unmoved_attraction(v, rowptr, colids, pold, batch, W);
 }
 
 
@@ -1409,12 +1409,7 @@ __global__ void __launch_bounds__(kTravThreads) traverse_kernel(TraverseArgs a) 
   const int v = a.perm[k];
   a.rep[v] = rep;
   // minus the repulsion into v's sum of unmoved neighbours' attraction
-  if (a.f0) {
-    float4 f = a.f0[v];  // {hx, hy, lx, ly}
-    ff_add(f.x, f.z, -rep.x);
-    ff_add(f.y, f.w, -rep.y);
-    a.f0[v] = f;
-  }
+  if (a.f0) a.f0[v] = bh_minus_repulsion(a.f0[v], rep);
   if (kStats) {  // one atomic per group of converged lanes, not per thread
     const unsigned int m = __activemask();
     const unsigned int sv = __reduce_add_sync(m, visits), se = __reduce_add_sync(m, exact);

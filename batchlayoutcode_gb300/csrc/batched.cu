@@ -615,7 +615,7 @@ __device__ void layout_bh(const BatchedArgs &a, int g, BhShared &S, double *red)
         const float2 rep = bh_repulsion<false>(nodes, c64, nlvl, maxmin, a.theta, total, spos[k], visits,
                                                exact);
         const int v = vin[k];
-        f0[v] = bh_unmoved_attraction(v, rep, rp, ci, pos, a.batch, a.W);
+        f0[v] = bh_minus_repulsion(bh_unmoved_attraction(v, rp, ci, pos, a.batch, a.W), rep);
       }
     }
     __syncthreads();

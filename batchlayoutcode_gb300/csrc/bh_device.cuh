@@ -242,15 +242,15 @@ __device__ __forceinline__ void bh_attract(float2 pj, float2 pv, float W, float 
   ff_add(hy, ly, dy * sc);
 }
 
-// Minus the repulsion plus the attraction of the neighbours j of v that are
-// not moved before v in this iteration (j at or after v's batch start), read
-// at their iteration-start positions; CSR order, float-float.
-__device__ __forceinline__ float4 bh_unmoved_attraction(int v, float2 rep, const int *__restrict__ rowptr,
+// The attraction of the neighbours j of v that are not moved before v in
+// this iteration (j at or after v's batch start), read at their
+// iteration-start positions; CSR order, float-float {hx, hy, lx, ly}.
+__device__ __forceinline__ float4 bh_unmoved_attraction(int v, const int *__restrict__ rowptr,
                                                         const int *__restrict__ colids, const float2 *pold, int batch,
                                                         float W) {
   const float2 pv = pold[v];
   const int batch_lo = (v / batch) * batch;
-  float hx = -rep.x, lx = 0.f, hy = -rep.y, ly = 0.f;
+  float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f;
   const int e1 = rowptr[v + 1];
   constexpr int kU = 4;  // index loads first, then position loads, then the ordered sum
   for (int e = rowptr[v]; e < e1; e += kU) {
@@ -268,6 +268,14 @@ __device__ __forceinline__ float4 bh_unmoved_attraction(int v, float2 rep, const
     }
   }
   return make_float4(hx, hy, lx, ly);
+}
+
+// f (float-float {hx, hy, lx, ly}) minus the repulsion: the sum the level
+// sweep starts from.
+__device__ __forceinline__ float4 bh_minus_repulsion(float4 f, float2 rep) {
+  ff_add(f.x, f.z, -rep.x);
+  ff_add(f.y, f.w, -rep.y);
+  return f;
 }
 
 // Unit-step update (algorithms.cpp:1062-1066) from the float-float force:
