@@ -1699,6 +1699,19 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta, int attract_batch) {
     ctx->launches++;
   }
   bl_time_end(ctx, "frame_morton");
+  // the walk's attraction part (for the iteration that follows) needs no
+  // tree: on the second stream (lower priority) beside the single-wave sort
+  // passes; before the frame kernel it slowed that cooperative launch
+  if (attract_batch > 0) {
+    const bool side = ctx->side && ctx->ev_fork && ctx->ev_join;
+    if (side) {
+      BL_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
+      BL_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+    }
+    unmoved_attraction_kernel<<<nblk(n, 256), 256, 0, side ? ctx->side : st>>>(
+        n, ctx->g.rowptr, ctx->g.colids, pos, attract_batch, (float)ctx->weight, s.f0);
+    ctx->launches++;
+  }
   bl_time_begin(ctx, "radix_sort");
   bl_time_begin(ctx, "lsd_passes");
   // bits 32..63 by four LSD passes, then the runs of equal high halves
@@ -1766,11 +1779,9 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta, int attract_batch) {
   bl_time_begin(ctx, "centroid_kernel");
   centroid_kernel<<<nblk(n, kCenSpan), kCenThreads, sizeof(CenSmem), st>>>(t);
   // the quad nodes spanning one boundary (one warp per boundary); then on the
-  // side stream (at the lower priority) the walk's attraction part and the
-  // records of the points and of the nodes spanning at most one boundary,
-  // beside the nodes spanning more (one cluster, which leaves most SMs free).
-  // (Started with the frame kernel instead, the attraction slowed that
-  // cooperative launch by more than it saved.)
+  // side stream (at the lower priority) the records of the points and of the
+  // nodes spanning at most one boundary, beside the nodes spanning more (one
+  // cluster, which leaves most SMs free)
   const bool fork = ctx->side && ctx->ev_fork && ctx->ev_join;
   const bool spans = ncb > 1;  // one block has no spanning node
   bl_time_begin(ctx, "centroid_top");
@@ -1781,11 +1792,6 @@ int bh_build(bl_ctx *ctx, const float2 *pos, double theta, int attract_batch) {
   if (fork) {
     BL_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
     BL_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-  }
-  if (attract_batch > 0) {  // the walk's attraction part (needs no tree), for the iteration that follows
-    unmoved_attraction_kernel<<<nblk(n, 256), 256, 0, fork ? ctx->side : st>>>(
-        n, ctx->g.rowptr, ctx->g.colids, pos, attract_batch, (float)ctx->weight, s.f0);
-    ctx->launches++;
   }
   layout_local_kernel<<<nblk(n, 256), 256, 0, fork ? ctx->side : st>>>(t);
   ctx->launches++;

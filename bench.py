@@ -212,7 +212,7 @@ def allpairs_fraction(B, torch, device: int, flush, iterations: int = 3) -> dict
 def bh_roofline(g, kernel, workload, visits, kernel_s, step_s, sm_mhz, pk):
     """Roofline of the Barnes-Hut traversal and of the whole step.
 
-    The traversal reads its tree records from L1/L2 (about 4 % of the record
+    The traversal reads its tree records from L1/L2 (under 1 % of the record
     bytes reach DRAM), so its bound is instruction issue: warp instructions
     per launch = live record visits x (warp instructions per visit of the
     committed ncu capture of this kernel), over 152 SMs x 4 schedulers x the
@@ -239,8 +239,8 @@ def bh_roofline(g, kernel, workload, visits, kernel_s, step_s, sm_mhz, pk):
                     "peak " + hbm_src}
     records = {"achieved": visits * 16.0 / kernel_s / 1e9, "unit": "GB/s", "bytes_per_launch": visits * 16.0,
                "frac_of_hbm": visits * 16.0 / kernel_s / 1e9 / hbm,
-               "note": "record visits x 16 B per launch over the traversal time; ~96 % of these bytes hit "
-                       "L1/L2, so this is not a DRAM figure"}
+               "note": "record visits x 16 B per launch over the traversal time; over 99 % of these bytes "
+                       "hit L1/L2, so this is not a DRAM figure"}
     if inst_prof and visits_prof:
         inst = visits * inst_prof / visits_prof
         peak = 152 * 4 * sm_mhz * 1e6 / 1e9
