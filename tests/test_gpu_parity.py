@@ -377,6 +377,41 @@ def test_rgg1m_traversal_decisions_exact(B, rgg1m, theta):
     assert rel_l2(rep, orep) <= FORCE_TOL
 
 
+@pytest.mark.parametrize("layout", ["uniform", "clustered", "ties", "tight", "n1025", "n2049"])
+def test_quadtree_layouts_bit_exact(B, layout):
+    """The quadtree (structure and every FP64 centroid) on the sort test's
+    layouts — long runs of equal keys that span centroid blocks ("ties"), a
+    20,000-point cluster that takes the tree 20-odd levels down ("tight") —
+    and on one or two block boundaries only (1,025 and 2,049 points: every
+    spanning node in one boundary's chain, none for the cluster pass).  The
+    repulsion too where no two points coincide."""
+    rng = np.random.default_rng(4)
+    n = {"n1025": 1025, "n2049": 2049}.get(layout, 60000)
+    if layout == "clustered":
+        xy = rng.normal(0, 1e-3, (n, 2))
+        xy[:8] = [[-5, -5], [5, 5], [-5, 5], [5, -5], [0, 5], [5, 0], [-5, 0], [0, -5]]
+    elif layout == "ties":
+        xy = rng.integers(0, 40, (n, 2)).astype(np.float64) * 0.125
+    elif layout == "tight":
+        xy = rng.uniform(-3, 3, (n, 2))
+        xy[:20000] = 1.0 + rng.uniform(0, 1e-6, (20000, 2))
+    else:
+        xy = rng.uniform(-3, 3, (n, 2))
+    xy = xy.astype(np.float32).astype(np.float64)
+    rowptr = np.zeros(n + 1, np.int32)
+    with B.Algorithms(rowptr, np.zeros(0, np.int32)) as a:
+        a.nCoordinates = xy
+        t = a.quadtree()
+        rep, (visits, _) = a.bh_repulsion(1.2)
+    ot = oracle.bh_tree(xy)
+    for k in ("lo", "hi", "depth", "nchild", "centroid"):
+        assert np.array_equal(t[k], ot[k]), k
+    if layout in ("uniform", "clustered", "n1025", "n2049"):
+        orep, ovis = oracle.bh_repulsion(xy, xy, 1.2, visits=True)
+        assert visits == int(ovis.sum())
+        assert rel_l2(rep, orep) <= FORCE_TOL
+
+
 def test_deep_tree_over_many_block_boundaries(B):
     """10M points on the line y = x: every quad cell splits in two, so the
     tree is binary and deep; ~9,750 of its nodes span two or more centroid
