@@ -1170,9 +1170,9 @@ __device__ __forceinline__ int span_level_of(const SpanLevels &L, int g) {
 
 // Staging of the listed nodes, one thread each, over the whole device (the
 // gathers of a node's children are scattered loads; on the cluster's few SMs
-// alone they queue): the node's position, and per child its centroid when it
-// is final (a point, or a node inside one block) or its node id when it is a
-// listed node itself.  A run of identical keys (children: points only) is
+// alone they queue): the node's position, its record's place, and per child
+// its centroid when it is final (a point, or a node within one block or
+// spanning one boundary) or its node id when it is a listed node itself.  A run of identical keys (children: points only) is
 // computed here.  Nothing is staged when the cluster cannot hold the nodes.
 __global__ void __launch_bounds__(kStageThreads) span_stage_kernel(TreeArgs t) {
   __shared__ SpanLevels L;
@@ -1257,8 +1257,9 @@ struct TopSmem {
 // block holding it, a cluster barrier after every round.  Every thread reads
 // the same level counts, so all take the same cluster barriers; every block
 // reads the error record before the first barrier and this kernel records
-// errors only after it, so all blocks leave together or none.  More listed
-// nodes than the blocks can hold: the same rounds through global memory.
+// errors only after it, so all blocks leave together or none.  Each block
+// then writes its nodes' centroids and pre-order records.  More listed nodes
+// than the blocks can hold: the same rounds through global memory.
 __global__ void __cluster_dims__(kTopCtas, 1, 1) __launch_bounds__(kTopThreads, 1)
     centroid_top_kernel(TreeArgs t) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
